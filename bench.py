@@ -1,0 +1,339 @@
+"""Benchmark: single-graph truss decomposition on one GB300 (edges/s).
+
+Workload (N=1): R-MAT scale 22, edge factor 16 (2^26 draws),
+(a,b,c,d) = (0.57, 0.19, 0.19, 0.05), seed 1, symmetrised, deduplicated and
+degree-oriented (int32 CSR, int64 row offsets).  A step = one full
+decomposition (support pass + every peel level + the e_truss/ptr_truss
+outputs) of that graph.
+
+* value: edges/s with the CSR resident in HBM (inputs larger than L2);
+* e2e:   the same through truss_decompose with host buffers: each step
+         copies rows/cols/row_ptr from pinned host memory and reads the
+         per-edge truss numbers back;
+* roofline: the dominant kernel's algorithmic bytes (B = 4W + 28E + 4(V+1),
+         W = sum over edges of d+(u)+d+(v)) over its CUDA-event time;
+* cpu_baseline: the oracle port of the reference's CPU flow (OpenMP, all host
+         cores) on a bounded R-MAT sample.
+
+--impl reference times the reference's CPU implementation (the oracle port,
+all host threads) on the same metric.  Multi-GPU (torchrun): replicas only;
+each rank decomposes its own copy, value = ranks * E / max step time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "edges/s decomposed"
+UNIT = "edges/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--cpu-scale", type=int, default=0, help="R-MAT scale of the CPU sample (0 = auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- distributed helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, backend):
+    import torch.distributed as dist
+    if ws > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+    return dist
+
+
+def max_over_ranks(x, ws, device):
+    import torch
+    import torch.distributed as dist
+    if ws == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    import torch.distributed as dist
+    if ws > 1:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=5)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU legs (oracle)
+def cpu_sample_scale(args, steps):
+    if args.cpu_scale:
+        return args.cpu_scale
+    return 17 if steps <= 15 else (16 if steps <= 40 else 15)
+
+
+def cpu_decompose_sample(scale, reps, warm=0):
+    """The oracle port of the reference's `--cuda` flow (singlegpu_truss.py
+    k_truss, OpenMP ops) on R-MAT(scale, 16*2^scale draws, seed 1)."""
+    import numpy as np
+    from oracle import oracle as O
+    from tdtdecomposition_gb300 import generators as G
+    s, d = G.rmat_edges(scale, 16 << scale, seed=1)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
+    V = len(verts)
+    rpt = O.tiling_row_ptr(rows, cols, V, 2)
+    for _ in range(warm):
+        O.k_truss(rows, cols, rpt, V, 2)
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        O.k_truss(rows, cols, rpt, V, 2)
+        times.append(time.perf_counter() - t)
+    return len(cols), V, times, O.num_threads()
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if ws > 1:
+        dist_init(ws, "gloo")
+        if rank != 0:
+            return
+    scale = cpu_sample_scale(args, args.steps + args.warmup)
+    E, V, times, threads = cpu_decompose_sample(scale, args.steps, args.warmup)
+    t = sum(times)
+    value = E * len(times) / t
+    sample = "R-MAT scale %d, 16*2^%d draws, seed 1 (V=%d, E=%d), one full decomposition per step" % (
+        scale, scale, V, E)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic",
+            "config": {"workload": "R-MAT single-graph truss decomposition (CPU sample of scale %d)" % scale,
+                       "scale": scale, "edge_factor": 16, "V": V, "E": E},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def main_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    dist_init(ws, "nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from tdtdecomposition_gb300 import _lib, generators as G, truss as T
+    from tdtdecomposition_gb300.preprocess import preprocess_edges, wedge_work
+    L = _lib.load()  # raises if the CUDA library is missing
+
+    scale, ef = args.scale, args.edge_factor
+    m = ef << scale
+    src, dst = G.rmat_edges_device(scale, m, seed=1, device=dev)
+    g, vertices = preprocess_edges(src, dst)
+    del src, dst
+    torch.cuda.synchronize()
+    V, E = g.num_vertices, g.num_edges
+    W = wedge_work(g)
+    B_sup = 4 * W + 28 * E + 4 * (V + 1)
+    wsp = T.Workspace(dev)
+
+    def step():
+        return T.truss_decompose(g, workspace=wsp, sync=False)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # correctness anchor of this run: stats of one decomposition
+    res = T.truss_decompose(g, workspace=wsp)
+
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    stream = torch.cuda.current_stream(dev)
+    L.tdt_profile_start(args.steps)
+    n0 = L.tdt_launch_count()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = L.tdt_launch_count() - n0
+    import ctypes
+    ms_s, ms_p, ms_o, nc = ctypes.c_float(), ctypes.c_float(), ctypes.c_float(), ctypes.c_int()
+    L.tdt_profile_stop(ctypes.byref(ms_s), ctypes.byref(ms_p), ctypes.byref(ms_o), ctypes.byref(nc))
+    clk = clocks.stop() if clocks else None
+    t_ms = ev0.elapsed_time(ev1)
+    t_ms = max_over_ranks(t_ms, ws, dev)
+    ms_step = t_ms / args.steps
+    value = ws * E / (ms_step / 1e3)
+
+    # e2e: host buffers through the public API
+    rows_h = g.rows.cpu().pin_memory()
+    cols_h = g.columns.cpu().pin_memory()
+    rp_h = g.row_ptr.cpu().pin_memory()
+    truss_h = torch.empty(E, dtype=torch.int32).pin_memory()
+    from tdtdecomposition_gb300 import CSRCOO
+    d_rows = torch.empty_like(g.rows)
+    d_cols = torch.empty_like(g.columns)
+    d_rp = torch.empty_like(g.row_ptr)
+
+    def e2e_step():
+        d_rows.copy_(rows_h, non_blocking=True)
+        d_cols.copy_(cols_h, non_blocking=True)
+        d_rp.copy_(rp_h, non_blocking=True)
+        tr, _, _, _ = T.truss_decompose(CSRCOO(columns=d_cols, row_ptr=d_rp, rows=d_rows), workspace=wsp,
+                                        sync=False)
+        truss_h.copy_(tr, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    te = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+    assert torch.equal(truss_h, res.truss.cpu()), "e2e result differs from the resident run"
+    e2e_value = ws * E / (te / args.steps / 1e3)
+    h2d = rows_h.numel() * 4 + cols_h.numel() * 4 + rp_h.numel() * 8
+    d2h = truss_h.numel() * 4
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    n = max(nc.value, 1)
+    t_sup = ms_s.value / n
+    t_peel = ms_p.value / n
+    kernels = {
+        "support_kernel": {"ms": t_sup, "bytes": B_sup, "gbs": B_sup / (t_sup / 1e3) / 1e9},
+        "peel_phase": {"ms": t_peel, "bytes": B_sup, "gbs": B_sup / (t_peel / 1e3) / 1e9},
+    }
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic_rmat.json")
+    if os.path.exists(tr_path):
+        try:
+            tj = json.load(open(tr_path))
+            traffic = tj.get(dom, {}).get("bytes_per_launch_full")
+        except Exception:
+            traffic = None
+    ach = kernels[dom]["gbs"]
+    roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "traffic": traffic, "peak_source": peak_src,
+            "per_kernel": {k: {"ms": round(v["ms"], 4), "achieved_gbs": round(v["gbs"], 1),
+                               "algorithmic_bytes": v["bytes"]} for k, v in kernels.items()},
+            "post_phase_ms": ms_o.value / n}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "R-MAT scale %d edge factor %d single-graph truss decomposition" % (scale, ef),
+                       "scale": scale, "edge_factor": ef, "abcd": [0.57, 0.19, 0.19, 0.05], "seed": 1,
+                       "V": V, "E": E, "W": W, "kmax": res.kmax, "triangles": res.triangles,
+                       "rounds": res.rounds, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (CSR %.0f MB + in-adjacency)" % ((8 * E + 8 * V) / 1e6)},
+            "roofline": roof,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": te / args.steps},
+            "gpu_launches": int(launches), "clocks": clk}
+    if not args.no_cpu_baseline:
+        sc = cpu_sample_scale(args, 1)
+        Ec, Vc, times, threads = cpu_decompose_sample(sc, 1)
+        line["cpu_baseline"] = {"value": Ec / times[0], "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "R-MAT scale %d, 16*2^%d draws, seed 1 (V=%d, E=%d), one full "
+                                          "decomposition, %.1f s" % (sc, sc, Vc, Ec, times[0])}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        main_ours(args)
+
+
+if __name__ == "__main__":
+    main()

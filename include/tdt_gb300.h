@@ -1,0 +1,232 @@
+/*
+ * tdt_gb300.h — C ABI of the GB300 (sm_103a) truss-decomposition library
+ * (libtdt_gb300.so).
+ *
+ * Conventions
+ *   - Every pointer argument is a DEVICE pointer unless its comment says host.
+ *   - The caller allocates every buffer, as with the reference's `trusstensor`
+ *     operators (the ops write their outputs in place and return nothing
+ *     there); here each call returns an int status (TDT_OK == 0) and never
+ *     allocates device memory itself.  Whole-path entry points take a
+ *     caller-provided workspace whose size the matching *_workspace_bytes()
+ *     query returns.
+ *   - Work is enqueued on `stream` (a cudaStream_t; NULL = the legacy default
+ *     stream, which is where the reference launches).  Calls are asynchronous;
+ *     device-side failures (a bounded wait that expired) are reported in the
+ *     device `stats` words described below.
+ *   - Graph layout: the degree-oriented CSRCOO of the reference
+ *     (src/type/CSRCOO.py:9-33): `rows`/`cols` int32[E] (edge i = rows[i] ->
+ *     cols[i]), columns sorted within each row, `row_ptr` of the rows.  The
+ *     drop-in operators take the reference's int32 tiled row_ptr
+ *     (int32[V*n_cut+1], singlegpu_truss.py:160-169); the whole-path entry
+ *     points take int64 row offsets int64[V+1] and require rows[i] < cols[i].
+ */
+#ifndef TDT_GB300_H
+#define TDT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *tdt_stream_t; /* == cudaStream_t */
+
+enum tdt_status {
+    TDT_OK = 0,
+    TDT_ERR_INVALID = 1,     /* bad argument (size, null pointer, n_cut < 1, ...) */
+    TDT_ERR_CUDA = 2,        /* a CUDA runtime call failed                       */
+    TDT_ERR_WORKSPACE = 3,   /* workspace smaller than *_workspace_bytes()       */
+    TDT_ERR_TIMEOUT = 4,     /* a bounded device-side wait expired               */
+    TDT_ERR_CAPACITY = 5,    /* an output capacity (e.g. ptr_truss_cap) too small */
+    TDT_ERR_UNSUPPORTED = 6, /* device or configuration not supported            */
+    TDT_ERR_NOT_ORIENTED = 7 /* an edge with rows[i] >= cols[i]                  */
+};
+
+/* Human-readable text of a status code, and detail of the last error raised
+ * on the calling host thread. */
+const char *tdt_status_string(int status);
+const char *tdt_last_error(void);
+int tdt_version(void);
+/* Number of kernels this library has launched in the process so far. */
+unsigned long long tdt_launch_count(void);
+
+/* Phase timing of the whole-path calls: after tdt_profile_start(n), the next
+ * n calls record CUDA events on their stream; tdt_profile_stop() waits for
+ * them and returns the summed milliseconds of the support kernel, of the
+ * peel phase (in-adjacency build, state init and the persistent peel kernel)
+ * and of the output phase, with the number of calls recorded (host pointers). */
+int tdt_profile_start(int max_calls);
+int tdt_profile_stop(float *ms_support, float *ms_peel, float *ms_post, int *ncalls);
+
+/* =====================================================================
+ * Drop-in `trusstensor` operators.
+ * Each replaces the pybind op of the same name in
+ * demo_truss/myops/mysrc/hpu_extension/myhpu_extension.cpp:572-593; the
+ * argument order is the reference's, with sizes made explicit.
+ * ===================================================================== */
+
+/* segment_add (myhpu_extension.cpp:8-16; kernel.cu:5-26):
+ * output[r] = sum(col_indices[col_ptr[r]:col_ptr[r+1]]) for every non-empty
+ * row r < num_rows; rows with an empty segment are left untouched.
+ * num_values = length of col_indices (segments are clamped to it). */
+int tdt_segment_add(const int32_t *col_indices, int64_t num_values, const int32_t *col_ptr,
+                    int32_t *output, int64_t num_rows, tdt_stream_t stream);
+
+/* segment_isin2 (myhpu_extension.cpp:24-34; kernel.cu:28-79) and
+ * segment_isin2tile (myhpu_extension.cpp:43-56; kernel.cu:81-141):
+ * output[i] += number of triangles containing edge i (its support).
+ * ACCUMULATES into output, as the reference does.  b_row_ptr holds
+ * row_ptr_len = V*n_cut+1 entries (n_cut = 1 for segment_isin2).
+ * Input contract (the reference's): a valid CSRCOO without -1 sentinels. */
+int tdt_segment_isin2(const int32_t *a_rows, const int32_t *b_col_indices,
+                      const int32_t *b_row_ptr, int64_t row_ptr_len, int32_t *output,
+                      int64_t num_edges, tdt_stream_t stream);
+int tdt_segment_isin2tile(const int32_t *a_rows, const int32_t *b_col_indices,
+                          const int32_t *b_row_ptr, int64_t row_ptr_len, int32_t n_cut,
+                          int32_t *output, int64_t num_edges, tdt_stream_t stream);
+
+/* sub_AllAffectedSupport (myhpu_extension.cpp:70-86; kernel.cu:144-191) and
+ * sub_AllAffectedSupport_tile (myhpu_extension.cpp:162-177; kernel.cu:407-456):
+ * `mark` = deleted edges.  For each affected edge e and each triangle of e
+ * whose third column is live (not -1) and that has a deleted edge: the two
+ * wedge edges still above l are decremented and flagged in n_mark; e, when
+ * not deleted, is decremented by the number of such triangles and flagged. */
+int tdt_sub_all_affected_support(const int32_t *e_affect, int64_t num_affect,
+                                 const int32_t *a_rows, const int32_t *b_col_indices,
+                                 const int32_t *b_row_ptr, int64_t row_ptr_len,
+                                 const uint8_t *mark, int32_t l, uint8_t *n_mark,
+                                 int32_t *output, int64_t num_edges, tdt_stream_t stream);
+int tdt_sub_all_affected_support_tile(const int32_t *e_affect, int64_t num_affect,
+                                      const int32_t *a_rows, const int32_t *b_col_indices,
+                                      const int32_t *b_row_ptr, int64_t row_ptr_len, int32_t n_cut,
+                                      const uint8_t *mark, int32_t l, uint8_t *n_mark,
+                                      int32_t *output, int64_t num_edges, tdt_stream_t stream);
+
+/* sub_AllAffectedSupport_not (myhpu_extension.cpp:93-106; kernel.cu:220-273)
+ * and sub_AllAffectedSupport_tilenot (myhpu_extension.cpp:191-205;
+ * kernel.cu:492-547), the peel update of the `--cuda` flow:
+ * `mark` = alive and not peeled this round.  A triangle of affected edge e
+ * with a live third column is destroyed when not all of its three edges are
+ * in `mark`: each wedge edge above l loses one and is flagged in n_mark when
+ * it reaches l; e, when in `mark`, loses the number of destroyed triangles
+ * and is flagged when it ends at or below l.  Supports that end at or below l
+ * are racy in the reference and here alike; n_mark and supports above l are
+ * exact. */
+int tdt_sub_all_affected_support_not(const int32_t *e_affect, int64_t num_affect,
+                                     const int32_t *a_rows, const int32_t *b_col_indices,
+                                     const int32_t *b_row_ptr, int64_t row_ptr_len,
+                                     const uint8_t *mark, int32_t l, uint8_t *n_mark,
+                                     int32_t *output, int64_t num_edges, tdt_stream_t stream);
+int tdt_sub_all_affected_support_tilenot(const int32_t *e_affect, int64_t num_affect,
+                                         const int32_t *a_rows, const int32_t *b_col_indices,
+                                         const int32_t *b_row_ptr, int64_t row_ptr_len,
+                                         int32_t n_cut, const uint8_t *mark, int32_t l,
+                                         uint8_t *n_mark, int32_t *output, int64_t num_edges,
+                                         tdt_stream_t stream);
+
+/* sub_AllAffectedSupport_notwin (myhpu_extension.cpp:123-140; kernel.cu:302-370)
+ * and _tilenotwin (myhpu_extension.cpp:224-242; kernel.cu:578-648): the _not
+ * update that also flags, in in_windows_mask, every edge whose support
+ * crosses below windows_high and appends its index to buff_index at
+ * atomicAdd(buf_size, 1).  buff_index must hold num_edges entries. */
+int tdt_sub_all_affected_support_notwin(const int32_t *e_affect, int64_t num_affect,
+                                        const int32_t *a_rows, const int32_t *b_col_indices,
+                                        const int32_t *b_row_ptr, int64_t row_ptr_len,
+                                        const uint8_t *mark, int32_t l, uint8_t *n_mark,
+                                        int32_t *output, int32_t windows_high,
+                                        uint8_t *in_windows_mask, int32_t *buff_index,
+                                        int32_t *buf_size, int64_t num_edges,
+                                        tdt_stream_t stream);
+int tdt_sub_all_affected_support_tilenotwin(const int32_t *e_affect, int64_t num_affect,
+                                            const int32_t *a_rows, const int32_t *b_col_indices,
+                                            const int32_t *b_row_ptr, int64_t row_ptr_len,
+                                            int32_t n_cut, const uint8_t *mark, int32_t l,
+                                            uint8_t *n_mark, int32_t *output,
+                                            int32_t windows_high, uint8_t *in_windows_mask,
+                                            int32_t *buff_index, int32_t *buf_size,
+                                            int64_t num_edges, tdt_stream_t stream);
+
+/* k-truss search operators.  The reference launches these from pycuda
+ * (ktruss_search/ktruss_cuda.py:316-343); they are not in its trusstensor
+ * module.  Mapping: run_kernel_two_k -> tdt_segment_isin2_k,
+ * run_kernel_two_tile_k -> tdt_segment_isin2tile_k, run_affect_support ->
+ * tdt_sub_affected_support, run_affect_support_tile ->
+ * tdt_sub_affected_support_tile.
+ *
+ * segment_isin2_k (ktruss_cuda.py:121-200): the support count that stops
+ * incrementing a target once it has reached k (accumulates into output).
+ * sub_affected_support (ktruss_cuda.py:201-286): on an extracted subgraph,
+ * every unmarked edge loses one per triangle that has a marked edge. */
+int tdt_segment_isin2_k(const int32_t *a_rows, const int32_t *b_col_indices,
+                        const int32_t *b_row_ptr, int64_t row_ptr_len, int32_t k,
+                        int32_t *output, int64_t num_edges, tdt_stream_t stream);
+int tdt_segment_isin2tile_k(const int32_t *a_rows, const int32_t *b_col_indices,
+                            const int32_t *b_row_ptr, int64_t row_ptr_len, int32_t n_cut,
+                            int32_t k, int32_t *output, int64_t num_edges, tdt_stream_t stream);
+int tdt_sub_affected_support(const int32_t *sub_rows, const int32_t *sub_columns,
+                             const int32_t *sub_row_ptr, int64_t row_ptr_len,
+                             const uint8_t *mark, int32_t *sub_support, int64_t num_edges,
+                             tdt_stream_t stream);
+int tdt_sub_affected_support_tile(const int32_t *sub_rows, const int32_t *sub_columns,
+                                  const int32_t *sub_row_ptr, int64_t row_ptr_len, int32_t n_cut,
+                                  const uint8_t *mark, int32_t *sub_support, int64_t num_edges,
+                                  tdt_stream_t stream);
+
+/* =====================================================================
+ * Whole-path entry points (the device-resident hot path).
+ * ===================================================================== */
+
+/* Layout of the int64 `stats` words the whole-path calls write (device). */
+enum tdt_stat_index {
+    TDT_STAT_STATUS = 0,     /* 0 = ok, else a tdt_status raised on the device */
+    TDT_STAT_KMAX = 1,       /* maximum truss number (2 for a triangle-free graph) */
+    TDT_STAT_NPTR = 2,       /* entries written to ptr_truss                   */
+    TDT_STAT_ROUNDS = 3,     /* peel sub-rounds executed                       */
+    TDT_STAT_TRIANGLES = 4,  /* triangle count                                 */
+    TDT_STAT_NETRUSS = 5,    /* entries written to e_truss                     */
+    TDT_STAT_ALIVE = 6,      /* k-truss search: edges left in the k-truss      */
+    TDT_STAT_COUNT = 8
+};
+
+/* Workspace for tdt_truss_decompose / tdt_ktruss_search / tdt_triangle_count. */
+size_t tdt_decompose_workspace_bytes(int64_t num_vertices, int64_t num_edges);
+
+/* Full truss decomposition: the single-call replacement of the `--cuda` flow
+ * k_truss (singlegpu_truss.py:67-158) together with its support pass
+ * (:38-45).  Outputs:
+ *   truss[E]      per-edge truss number (2 = in no triangle);
+ *   e_truss[E]    the reference's peel order: edges of level 1, 2, ... with,
+ *                 within each sub-round, ascending edge index (support-0 edges
+ *                 are not listed, as in the reference) — may be NULL;
+ *   ptr_truss     per-level offsets into e_truss (ptr_truss[0] = 0; level i
+ *                 = truss i+2 spans ptr_truss[i-1]..ptr_truss[i]); capacity
+ *                 ptr_truss_cap entries, may be NULL;
+ *   stats[8]      see tdt_stat_index (kmax = truss number of the last level).
+ * `rows` may be NULL (derived from row_ptr).  Requires rows[i] < cols[i]. */
+int tdt_truss_decompose(const int32_t *rows, const int32_t *cols, const int64_t *row_ptr,
+                        int64_t num_vertices, int64_t num_edges, int32_t *truss,
+                        int32_t *e_truss, int32_t *ptr_truss, int64_t ptr_truss_cap,
+                        int64_t *stats, void *workspace, size_t workspace_bytes,
+                        tdt_stream_t stream);
+
+/* Triangle count: support[E] (overwritten, may be NULL) and
+ * stats[TDT_STAT_TRIANGLES] = sum(support) / 3 (kernel.cu:28-79 semantics;
+ * the reference derives the count as support.sum() // 3). */
+int tdt_triangle_count(const int32_t *cols, const int64_t *row_ptr, int64_t num_vertices,
+                       int64_t num_edges, int32_t *support, int64_t *stats, void *workspace,
+                       size_t workspace_bytes, tdt_stream_t stream);
+
+/* k-truss search (ktruss_search/ktruss_cuda.py:383-463 with l = k-2):
+ * in_ktruss[i] = 1 when edge i belongs to the k-truss, else 0;
+ * stats[TDT_STAT_ALIVE] = its edge count. */
+int tdt_ktruss_search(const int32_t *rows, const int32_t *cols, const int64_t *row_ptr,
+                      int64_t num_vertices, int64_t num_edges, int32_t k, uint8_t *in_ktruss,
+                      int64_t *stats, void *workspace, size_t workspace_bytes,
+                      tdt_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TDT_GB300_H */

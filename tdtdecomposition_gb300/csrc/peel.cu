@@ -1,0 +1,672 @@
+// Device-resident truss decomposition and k-truss search.
+//
+// Replaces the `--cuda` flow's Python peel loop (singlegpu_truss.py:67-158:
+// ~12 torch launches and ~6 host syncs per sub-round, each O(E)) by ONE
+// persistent cooperative kernel that runs every sub-round and level on the
+// device, separated by a bounded grid barrier.
+//
+// Per sub-round r at level l, F_r = edges peeled in r (rnd[e] == r):
+//   * every e in F_r enumerates its triangles from the endpoint x of lower
+//     degree: the candidates are x's out- and in-neighbours w; the third edge
+//     between w and the other endpoint y is found by binary search in the
+//     sorted out-list of min(w, y) (ids are degree ranks, so that list is
+//     short);
+//   * a triangle (e, f, g) whose edges were all alive at the start of r is
+//     destroyed; f and g outside F_r lose one support each; when f (or g) is
+//     also in F_r only the member with the smaller index decrements the third
+//     edge; when all three are in F_r nothing is decremented;
+//   * an edge whose support drops from l+1 to l joins F_{r+1}.
+// When F_{r+1} is empty, the level advances to the minimum support of the
+// alive edges and F_{r+1} = alive edges with that support.
+// This yields exactly the reference's sub-round sets (singlegpu_truss.py:
+// 99-152 with sub_AllAffectedSupport_tilenot, kernel.cu:492-547): each
+// non-peeled edge loses one support per destroyed triangle, and an edge
+// joins the next sub-round exactly when its support reaches <= l; so
+// truss[e] = level + 2 and the reference's e_truss order (sub-rounds in
+// order, ascending edge index within a sub-round) are reproduced exactly.
+//
+// Work in a sub-round is a flat candidate space: each queued edge owns
+// deg(x) consecutive candidate slots (reserved with one packed 64-bit atomic
+// per warp: item count in the high bits, candidate count in the low bits, so
+// item order equals slot order), and every lane of the grid takes one slot
+// per step.  Hub edges therefore spread over all SMs instead of one thread.
+#include "common.cuh"
+#include "sort.cuh"
+
+namespace tdt {
+
+constexpr int kPeelBlock = 512;
+constexpr int kPeelWarps = kPeelBlock / kWarp;
+constexpr int kItemBits = 28;
+constexpr int kCandBits = 36;
+constexpr unsigned long long kCandMask = (1ull << kCandBits) - 1ull;
+// Wall-clock budget of one persistent peel launch; past it the run stops with
+// TDT_ERR_TIMEOUT instead of holding the GPU.
+constexpr uint64_t kPeelDeadlineNs = 120ull * 1000ull * 1000ull * 1000ull;
+
+struct PeelCtl {
+    GridCtl g;
+    unsigned long long q[3];      // packed (items << kCandBits | candidates) per round slot
+    unsigned long long fe[3];     // frontier edges per round slot (queued or not)
+    int min_sup[2];
+    int level;
+    int pad0;
+    long long rounds;
+    long long triangles;
+    unsigned long long alive;
+};
+
+struct PeelArgs {
+    const int64_t* rp;
+    const int32_t* cols;
+    const int32_t* rows;
+    const int64_t* cp;
+    const int32_t* in_src;
+    const int32_t* in_eid;
+    int32_t* sup;
+    int32_t* rnd;
+    int32_t* round_level;
+    int4* qi[2];
+    long long* qb[2];
+    int64_t V, E, round_cap;
+    int32_t mode;         // 0: full decomposition, 1: fixed-level peel (k-truss search)
+    int32_t fixed_level;
+    PeelCtl* ctl;
+};
+
+__device__ __forceinline__ void set_status(PeelCtl* c, int s) {
+    atomicMax(&c->g.status, s);
+    atomicExch(&c->g.abort, 1);
+}
+
+__device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long* p) {
+    return __ldcg(p);
+}
+
+// Queue the edges flagged by `want` (one per lane) for the round in `slot`.
+// cur_sup is the edge's support at marking time (0 => no alive triangle).
+__device__ __forceinline__ void warp_append(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
+                                            int32_t cur_sup) {
+    const unsigned lane = lane_id();
+    const unsigned mf = __ballot_sync(kFull, want);
+    if (mf == 0) return;
+    if (lane == (unsigned)(__ffs(mf) - 1)) atomicAdd(&A.ctl->fe[slot], (unsigned long long)__popc(mf));
+    int32_t x = 0, y = 0, dxo = 0;
+    long long dx = 0;
+    bool q = want && cur_sup > 0;
+    if (q) {
+        const int32_t u = __ldg(A.rows + e), v = __ldg(A.cols + e);
+        const long long duo = __ldg(A.rp + u + 1) - __ldg(A.rp + u);
+        const long long du = duo + __ldg(A.cp + u + 1) - __ldg(A.cp + u);
+        const long long dvo = __ldg(A.rp + v + 1) - __ldg(A.rp + v);
+        const long long dv = dvo + __ldg(A.cp + v + 1) - __ldg(A.cp + v);
+        if (du <= dv) { x = u; y = v; dx = du; dxo = (int32_t)duo; }
+        else { x = v; y = u; dx = dv; dxo = (int32_t)dvo; }
+        if (dx <= 1) q = false;
+    }
+    const unsigned m = __ballot_sync(kFull, q);
+    if (m == 0) return;
+    const long long c = q ? dx : 0;
+    const long long incl = warp_incl_scan(c);
+    const long long tot = __shfl_sync(kFull, incl, 31);
+    const int n = __popc(m);
+    unsigned long long old = 0;
+    if (lane == 0) {
+        old = atomicAdd(&A.ctl->q[slot], ((unsigned long long)n << kCandBits) + (unsigned long long)tot);
+        const unsigned long long it0 = old >> kCandBits, c0 = old & kCandMask;
+        if (it0 + n >= (1ull << kItemBits) || c0 + tot >= (1ull << kCandBits) || (long long)(it0 + n) > A.E)
+            set_status(A.ctl, TDT_ERR_CAPACITY);
+    }
+    old = __shfl_sync(kFull, old, 0);
+    if (q) {
+        const long long it0 = (long long)(old >> kCandBits), c0 = (long long)(old & kCandMask);
+        const long long idx = it0 + __popc(m & lanemask_lt());
+        if (idx < A.E) {
+            A.qi[buf][idx] = make_int4(e, x, y, dxo);
+            A.qb[buf][idx] = c0 + incl - c;
+        }
+    }
+}
+
+// One decrement; returns true when the edge crossed from l+1 to l.
+__device__ __forceinline__ bool dec_support(const PeelArgs& A, int64_t x, int32_t l, int r_next) {
+    const int32_t old = atomicSub(A.sup + x, 1);
+    if (old == l + 1) {
+        A.rnd[x] = r_next;
+        return true;
+    }
+    return false;
+}
+
+// Level transition (decomposition mode): l = min support over alive edges,
+// F_{r_next} = alive edges with support l.  Returns false when no edge is alive.
+__device__ bool level_transition(const PeelArgs& A, int r_next, int ntrans, int32_t* l_out) {
+    __shared__ int s_min[kPeelWarps];
+    const unsigned lane = lane_id();
+    const int wib = threadIdx.x / kWarp;
+    const int p = ntrans & 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl->min_sup[p ^ 1] = INT32_MAX;
+    int mn = INT32_MAX;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < A.E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        if (__ldcg(A.rnd + e) == -1) {
+            const int32_t s = __ldcg(A.sup + e);
+            mn = s < mn ? s : mn;
+        }
+    }
+    mn = warp_min(mn);
+    if (lane == 0) s_min[wib] = mn;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int b = INT32_MAX;
+        for (int i = 0; i < kPeelWarps; i++) b = s_min[i] < b ? s_min[i] : b;
+        if (b != INT32_MAX) atomicMin(&A.ctl->min_sup[p], b);
+    }
+    if (!grid_barrier(&A.ctl->g, gridDim.x)) return false;
+    const int l = *(volatile int*)&A.ctl->min_sup[p];
+    if (l == INT32_MAX) return false;
+    *l_out = l;
+    const int slot = r_next % 3, buf = r_next & 1;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; base < A.E;
+         base += nthreads) {
+        const int64_t e = base + lane;
+        bool want = false;
+        int32_t s = 0;
+        if (e < A.E && __ldcg(A.rnd + e) == -1) {
+            s = __ldcg(A.sup + e);
+            if (s <= l) { want = true; A.rnd[e] = r_next; }
+        }
+        warp_append(A, slot, buf, want, (int32_t)e, s);
+    }
+    return grid_barrier(&A.ctl->g, gridDim.x);
+}
+
+// Fixed-level start (k-truss search): F_0 = edges with support <= l.
+__device__ bool fixed_start(const PeelArgs& A, int32_t l) {
+    const unsigned lane = lane_id();
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; base < A.E;
+         base += nthreads) {
+        const int64_t e = base + lane;
+        bool want = false;
+        int32_t s = 0;
+        if (e < A.E) {
+            s = __ldcg(A.sup + e);
+            if (s <= l) { want = true; A.rnd[e] = 0; }
+        }
+        warp_append(A, 0, 0, want, (int32_t)e, s);
+    }
+    return grid_barrier(&A.ctl->g, gridDim.x);
+}
+
+__global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
+    __shared__ long long s_win[kPeelWarps][kWarp];
+    const unsigned lane = lane_id();
+    const int wib = threadIdx.x / kWarp;
+    const int64_t gwarp = (int64_t)blockIdx.x * kPeelWarps + wib;
+    const int64_t nwarps = (int64_t)gridDim.x * kPeelWarps;
+    const bool master = blockIdx.x == 0 && threadIdx.x == 0;
+
+    if (*(volatile int*)&A.ctl->g.status != 0) return;  // invalid input was detected
+    const uint64_t t_start = globaltimer_ns();
+    int r = 0;
+    int32_t l = 0;
+    int ntrans = 0;
+    bool ok;
+    if (A.mode == 0) {
+        ok = level_transition(A, 0, ntrans++, &l);
+    } else {
+        l = A.fixed_level;
+        ok = fixed_start(A, l);
+    }
+    if (!ok) {
+        if (master) A.ctl->rounds = 0;
+        return;
+    }
+    for (;;) {
+        if (master) {
+            A.round_level[r] = l;
+            A.ctl->q[(r + 2) % 3] = 0;
+            A.ctl->fe[(r + 2) % 3] = 0;
+            if (globaltimer_ns() - t_start > kPeelDeadlineNs) set_status(A.ctl, TDT_ERR_TIMEOUT);
+        }
+        const int slot = r % 3, buf = r & 1;
+        const int nslot = (r + 1) % 3, nbuf = buf ^ 1;
+        const unsigned long long packed = ld_cg_u64(&A.ctl->q[slot]);
+        const long long N = (long long)(packed >> kCandBits);
+        const long long T = (long long)(packed & kCandMask);
+        const long long* __restrict__ qb = A.qb[buf];
+        const int4* __restrict__ qi = A.qi[buf];
+        for (long long cb = gwarp * kWarp; cb < T; cb += nwarps * kWarp) {
+            // item owning slot cb: last i with qb[i] <= cb
+            long long i0 = 0;
+            if (lane == 0) {
+                long long lo = 0, hi = N - 1;
+                while (lo < hi) {
+                    long long mid = (lo + hi + 1) >> 1;
+                    if (__ldcg(qb + mid) <= cb) lo = mid; else hi = mid - 1;
+                }
+                i0 = lo;
+            }
+            i0 = __shfl_sync(kFull, i0, 0);
+            s_win[wib][lane] = (i0 + lane < N) ? __ldcg(qb + i0 + lane) : LLONG_MAX;
+            __syncwarp();
+            const long long t = cb + lane;
+            bool want_f = false, want_g = false;
+            int64_t f = 0, g = 0;
+            if (t < T) {
+                int lo = 0, hi = 31;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (s_win[wib][mid] <= t) lo = mid; else hi = mid - 1;
+                }
+                const long long item = i0 + lo;
+                const int4 it = __ldcg(qi + item);
+                const int32_t e = it.x, x = it.y, y = it.z, dxo = it.w;
+                const long long tl = t - s_win[wib][lo];
+                int32_t w;
+                if (tl < dxo) {
+                    f = __ldg(A.rp + x) + tl;
+                    w = __ldg(A.cols + f);
+                } else {
+                    const int64_t k = __ldg(A.cp + x) + (tl - dxo);
+                    w = __ldg(A.in_src + k);
+                    f = __ldg(A.in_eid + k);
+                }
+                if (w != y) {
+                    g = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
+                                : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
+                    if (g >= 0) {
+                        const int32_t rf = __ldcg(A.rnd + f), rg = __ldcg(A.rnd + g);
+                        const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
+                        if (af && ag) {
+                            const bool ff = rf == r, fg = rg == r;
+                            if (!ff && !fg) {
+                                want_f = dec_support(A, f, l, r + 1);
+                                want_g = dec_support(A, g, l, r + 1);
+                            } else if (ff && !fg) {
+                                if (e < f) want_g = dec_support(A, g, l, r + 1);
+                            } else if (!ff && fg) {
+                                if (e < g) want_f = dec_support(A, f, l, r + 1);
+                            }
+                        }
+                    }
+                }
+            }
+            warp_append(A, nslot, nbuf, want_f, (int32_t)f, l);
+            warp_append(A, nslot, nbuf, want_g, (int32_t)g, l);
+            __syncwarp();
+        }
+        if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
+        if (r + 2 >= A.round_cap) {
+            if (master) set_status(A.ctl, TDT_ERR_CAPACITY);
+            return;
+        }
+        const unsigned long long nfe = ld_cg_u64(&A.ctl->fe[nslot]);
+        if (nfe == 0) {
+            if (A.mode != 0) break;
+            int32_t nl;
+            if (!level_transition(A, r + 1, ntrans++, &nl)) break;
+            l = nl;
+        }
+        r++;
+    }
+    if (master) A.ctl->rounds = r + 1;
+}
+
+// ------------------------------------------------------------------ setup / output kernels
+__global__ void rows_from_rp_kernel(const int64_t* __restrict__ rp, int64_t V, int32_t* __restrict__ rows) {
+    const unsigned lane = lane_id();
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < V; u += nw) {
+        const int64_t b = rp[u], e = rp[u + 1];
+        for (int64_t i = b + lane; i < e; i += kWarp) rows[i] = (int32_t)u;
+    }
+}
+
+// Input validation, before any kernel indexes through the graph:
+// row_ptr[0] == 0, row_ptr[V] == E, non-decreasing; rows[e] is the row that
+// owns position e; u < v < V; columns strictly increasing within a row.
+__global__ void validate_kernel(const int64_t* __restrict__ rp, const int32_t* __restrict__ rows,
+                                const int32_t* __restrict__ cols, int64_t E, int64_t V, PeelCtl* ctl) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    if (tid == 0 && (rp[0] != 0 || rp[V] != E)) atomicMax(&ctl->g.status, (int)TDT_ERR_INVALID);
+    for (int64_t u = tid; u < V; u += nth)
+        if (rp[u] > rp[u + 1]) atomicMax(&ctl->g.status, (int)TDT_ERR_INVALID);
+    for (int64_t e = tid; e < E; e += nth) {
+        const int32_t u = rows[e], v = cols[e];
+        if (u < 0 || u >= V || v >= V || u >= v) {
+            atomicMax(&ctl->g.status, (int)TDT_ERR_NOT_ORIENTED);
+            continue;
+        }
+        const int64_t b = rp[u], en = rp[u + 1];
+        if (e < b || e >= en) {
+            atomicMax(&ctl->g.status, (int)TDT_ERR_INVALID);
+            continue;
+        }
+        if (e + 1 < en && cols[e + 1] <= v) atomicMax(&ctl->g.status, (int)TDT_ERR_INVALID);
+    }
+}
+
+__global__ void indeg_kernel(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t E,
+                             int64_t V, int32_t* __restrict__ indeg, const PeelCtl* ctl) {
+    if (*(volatile const int*)&ctl->g.status != 0) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(indeg + cols[e], 1);
+}
+
+__global__ void csc_fill_kernel(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t E,
+                                int64_t V, const int64_t* __restrict__ cp, int32_t* __restrict__ cursor,
+                                int32_t* __restrict__ in_src, int32_t* __restrict__ in_eid, const PeelCtl* ctl) {
+    if (*(volatile const int*)&ctl->g.status != 0) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = rows[e], v = cols[e];
+        const int64_t pos = cp[v] + atomicAdd(cursor + v, 1);
+        in_src[pos] = u;
+        in_eid[pos] = (int32_t)e;
+    }
+}
+
+__global__ void init_state_kernel(const int32_t* __restrict__ sup, int32_t* __restrict__ rnd, int64_t E,
+                                  PeelCtl* ctl) {
+    __shared__ long long s_part[32];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->min_sup[0] = INT32_MAX;
+        ctl->min_sup[1] = INT32_MAX;
+    }
+    long long acc = 0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        rnd[e] = -1;
+        acc += sup[e];
+    }
+    acc = warp_sum(acc);
+    if (lane_id() == 0) s_part[threadIdx.x / kWarp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long b = 0;
+        for (int i = 0; i < (int)(blockDim.x / kWarp); i++) b += s_part[i];
+        atomicAdd((unsigned long long*)&ctl->triangles, (unsigned long long)b);
+    }
+}
+
+__global__ void truss_out_kernel(const int32_t* __restrict__ rnd, const int32_t* __restrict__ round_level,
+                                 int64_t E, int32_t* __restrict__ truss, uint32_t* __restrict__ keys,
+                                 uint32_t* __restrict__ vals, PeelCtl* ctl) {
+    if (ctl->g.status != 0) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = rnd[e];
+        if (r < 0) {  // every edge is peeled when the run completes
+            atomicMax((int*)&ctl->g.status, (int)TDT_ERR_CAPACITY);
+            continue;
+        }
+        if (truss) truss[e] = round_level[r] + 2;
+        keys[e] = (uint32_t)r;
+        vals[e] = (uint32_t)e;
+    }
+}
+
+// Number of sorted positions whose round has level <= lv (levels are
+// non-decreasing in round order).
+__device__ __forceinline__ int64_t count_level_le(const uint32_t* keys, int64_t E, const int32_t* round_level,
+                                                  int32_t lv) {
+    int64_t lo = 0, hi = E;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (round_level[keys[mid]] <= lv) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void ptr_etruss_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t E,
+                                  const int32_t* __restrict__ round_level, int32_t* __restrict__ ptr_truss,
+                                  int64_t ptr_cap, int32_t* __restrict__ e_truss, PeelCtl* ctl,
+                                  int64_t* __restrict__ stats) {
+    if (*(volatile int*)&ctl->g.status != 0) return;
+    const long long rounds = ctl->rounds;
+    const int32_t L = rounds > 0 ? round_level[rounds - 1] : 0;
+    const int64_t n0 = rounds > 0 ? count_level_le(keys, E, round_level, 0) : E;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    if (ptr_truss) {
+        if ((int64_t)L + 1 > ptr_cap) {
+            if (tid == 0) atomicMax(&ctl->g.status, (int)TDT_ERR_CAPACITY);
+        } else {
+            for (int64_t i = tid; i <= L; i += nth)
+                ptr_truss[i] = (int32_t)((i == 0 ? n0 : count_level_le(keys, E, round_level, (int32_t)i)) - n0);
+        }
+    }
+    if (e_truss)
+        for (int64_t p = n0 + tid; p < E; p += nth) e_truss[p - n0] = (int32_t)vals[p];
+    if (tid == 0) {
+        stats[TDT_STAT_KMAX] = (long long)L + 2;
+        stats[TDT_STAT_NPTR] = (long long)L + 1;
+        stats[TDT_STAT_ROUNDS] = rounds;
+        stats[TDT_STAT_TRIANGLES] = ctl->triangles / 3;
+        stats[TDT_STAT_NETRUSS] = E - n0;
+    }
+}
+
+__global__ void ktruss_out_kernel(const int32_t* __restrict__ rnd, int64_t E, uint8_t* __restrict__ in_k,
+                                  PeelCtl* ctl) {
+    __shared__ unsigned long long s_part[32];
+    unsigned long long acc = 0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t a = rnd[e] == -1;
+        in_k[e] = a;
+        acc += a;
+    }
+    acc = warp_sum(acc);
+    if (lane_id() == 0) s_part[threadIdx.x / kWarp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long b = 0;
+        for (int i = 0; i < (int)(blockDim.x / kWarp); i++) b += s_part[i];
+        atomicAdd(&ctl->alive, b);
+    }
+}
+
+__global__ void stats_final_kernel(PeelCtl* ctl, int64_t* stats, int mode) {
+    stats[TDT_STAT_STATUS] = ctl->g.status;
+    if (mode != 0) {
+        stats[TDT_STAT_ALIVE] = (long long)ctl->alive;
+        stats[TDT_STAT_ROUNDS] = ctl->rounds;
+        stats[TDT_STAT_TRIANGLES] = ctl->triangles / 3;
+    }
+}
+
+// ------------------------------------------------------------------ host side
+void prof_mark(int phase, cudaStream_t st);
+int launch_support_i64(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* out, void* ctl,
+                       const int* gate, cudaStream_t st);
+
+namespace {
+struct Carver {
+    char* base;
+    size_t off = 0;
+    size_t cap;
+    void* take(size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        void* p = base ? base + off : nullptr;
+        off += bytes;
+        return p;
+    }
+};
+
+struct Layout {
+    PeelCtl* ctl;
+    void* sup_ctl;
+    int32_t* rows_d;
+    int32_t* indeg;
+    int64_t* cp;
+    int32_t* in_src;
+    int32_t* in_eid;
+    int32_t* sup;
+    int32_t* rnd;
+    int32_t* round_level;
+    int4* qi[2];
+    long long* qb[2];
+    void* scan_ws;
+    void* sort_ws;
+    size_t total;
+};
+
+Layout carve(void* ws, int64_t V, int64_t E) {
+    Carver c{reinterpret_cast<char*>(ws)};
+    Layout L;
+    const size_t e = (size_t)(E > 0 ? E : 1), v = (size_t)(V > 0 ? V : 1);
+    L.ctl = (PeelCtl*)c.take(4096);
+    L.sup_ctl = c.take(256);
+    L.rows_d = (int32_t*)c.take(4 * e);
+    L.indeg = (int32_t*)c.take(4 * v);
+    L.cp = (int64_t*)c.take(8 * (v + 1));
+    L.in_src = (int32_t*)c.take(4 * e);
+    L.in_eid = (int32_t*)c.take(4 * e);
+    L.sup = (int32_t*)c.take(4 * e);
+    L.rnd = (int32_t*)c.take(4 * e);
+    L.round_level = (int32_t*)c.take(4 * (e + 2));
+    for (int b = 0; b < 2; b++) {
+        L.qi[b] = (int4*)c.take(16 * e);
+        L.qb[b] = (long long*)c.take(8 * e);
+    }
+    size_t scan_b = scan_scratch_bytes((int64_t)v + 1);
+    L.scan_ws = c.take(scan_b);
+    L.sort_ws = c.take(radix_sort_scratch_bytes((int64_t)e));
+    L.total = c.off + 256;
+    return L;
+}
+}  // namespace
+
+size_t decompose_workspace_bytes(int64_t V, int64_t E) {
+    // the e_truss sort reuses the queue buffers for its keys/values
+    return carve(nullptr, V, E).total;
+}
+
+// mode 0: decomposition; 1: k-truss search at level fixed_level; 2: support / triangle count only.
+int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* rp, int64_t V, int64_t E,
+             int32_t fixed_level, int32_t* truss, int32_t* e_truss, int32_t* ptr_truss, int64_t ptr_cap,
+             uint8_t* in_k, int32_t* support_out, int64_t* stats, void* ws, size_t ws_bytes, cudaStream_t st) {
+    TDT_CHECK_ARG(V >= 0 && E >= 0, "negative graph size");
+    TDT_CHECK_ARG(E < (int64_t)INT32_MAX, "num_edges %lld exceeds int32 edge ids", (long long)E);
+    TDT_CHECK_ARG(V < (int64_t)INT32_MAX, "num_vertices %lld exceeds int32 vertex ids", (long long)V);
+    TDT_CHECK_ARG(stats != nullptr, "stats is required");
+    TDT_CHECK_ARG(E == 0 || (cols && rp), "null graph pointer");
+    const size_t need = decompose_workspace_bytes(V, E);
+    if (ws_bytes < need || ws == nullptr) {
+        set_error("workspace of %zu bytes < required %zu", ws_bytes, need);
+        return TDT_ERR_WORKSPACE;
+    }
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    Layout L = carve(ws, V, E);
+    TDT_CUDA(cudaMemsetAsync(L.ctl, 0, 4096, st));
+    TDT_CUDA(cudaMemsetAsync(stats, 0, sizeof(int64_t) * TDT_STAT_COUNT, st));
+    if (E == 0) {
+        if (mode == 0) {
+            if (ptr_truss && ptr_cap >= 1) TDT_CUDA(cudaMemsetAsync(ptr_truss, 0, 4, st));
+            int64_t h[TDT_STAT_COUNT] = {0, 2, 1, 0, 0, 0, 0, 0};
+            if (ptr_truss && ptr_cap < 1) h[0] = TDT_ERR_CAPACITY;
+            TDT_CUDA(cudaMemcpyAsync(stats, h, sizeof(h), cudaMemcpyHostToDevice, st));
+            TDT_CUDA(cudaStreamSynchronize(st));
+        }
+        return TDT_OK;
+    }
+    const int tb = 256;
+    const unsigned g_e = grid_for(E, tb, di.sms, 8);
+    const int32_t* rows_use = rows;
+    if (!rows_use) {
+        rows_from_rp_kernel<<<grid_for(V * 32, tb, di.sms, 8), tb, 0, st>>>(rp, V, L.rows_d);
+        TDT_LAUNCH_CHECK("rows_from_rp");
+        rows_use = L.rows_d;
+    }
+    validate_kernel<<<g_e, tb, 0, st>>>(rp, rows_use, cols, E, V, L.ctl);
+    TDT_LAUNCH_CHECK("validate");
+    // support (skipped on the device when validation failed)
+    TDT_CUDA(cudaMemsetAsync(L.sup, 0, 4 * (size_t)E, st));
+    prof_mark(0, st);
+    rc = launch_support_i64(rp, cols, V, E, L.sup, L.sup_ctl, &L.ctl->g.status, st);
+    if (rc) return rc;
+    prof_mark(1, st);
+    if (mode == 2) {
+        init_state_kernel<<<g_e, tb, 0, st>>>(L.sup, L.rnd, E, L.ctl);
+        TDT_LAUNCH_CHECK("init_state");
+        if (support_out) TDT_CUDA(cudaMemcpyAsync(support_out, L.sup, 4 * (size_t)E, cudaMemcpyDeviceToDevice, st));
+        stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 1);
+        TDT_LAUNCH_CHECK("stats_final");
+        prof_mark(2, st);
+        prof_mark(3, st);
+        return TDT_OK;
+    }
+    // in-adjacency (CSC) of the oriented graph
+    TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
+    indeg_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.indeg, L.ctl);
+    TDT_LAUNCH_CHECK("indeg");
+    rc = exclusive_scan<int32_t, int64_t>(L.indeg, L.cp, V, L.cp + V, L.scan_ws, st);
+    if (rc) return rc;
+    TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
+    csc_fill_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.cp, L.indeg, L.in_src, L.in_eid, L.ctl);
+    TDT_LAUNCH_CHECK("csc_fill");
+    init_state_kernel<<<g_e, tb, 0, st>>>(L.sup, L.rnd, E, L.ctl);
+    TDT_LAUNCH_CHECK("init_state");
+
+    // persistent peel
+    int occ = 0;
+    TDT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, kPeelBlock, 0));
+    if (occ < 1) {
+        set_error("peel kernel cannot be resident");
+        return TDT_ERR_UNSUPPORTED;
+    }
+    PeelArgs A;
+    A.rp = rp; A.cols = cols; A.rows = rows_use; A.cp = L.cp; A.in_src = L.in_src; A.in_eid = L.in_eid;
+    A.sup = L.sup; A.rnd = L.rnd; A.round_level = L.round_level;
+    A.qi[0] = L.qi[0]; A.qi[1] = L.qi[1]; A.qb[0] = L.qb[0]; A.qb[1] = L.qb[1];
+    A.V = V; A.E = E; A.round_cap = E + 2;
+    A.mode = mode == 0 ? 0 : 1;
+    A.fixed_level = fixed_level;
+    A.ctl = L.ctl;
+    dim3 grid(di.sms * occ), block(kPeelBlock);
+    void* args[] = {&A};
+    // the peel phase also covers the CSC build and state init launched above
+    TDT_CUDA(cudaLaunchCooperativeKernel((void*)peel_kernel, grid, block, args, 0, st));
+    note_launch();
+    prof_mark(2, st);
+
+    if (mode == 0) {
+        // outputs: truss numbers, then e_truss / ptr_truss from a stable sort by round
+        uint32_t* keys = reinterpret_cast<uint32_t*>(L.qi[0]);
+        uint32_t* vals = keys + E;
+        uint32_t* keys_alt = reinterpret_cast<uint32_t*>(L.qi[1]);
+        uint32_t* vals_alt = keys_alt + E;
+        truss_out_kernel<<<g_e, tb, 0, st>>>(L.rnd, L.round_level, E, truss, keys, vals, L.ctl);
+        TDT_LAUNCH_CHECK("truss_out");
+        const uint32_t* sk = keys;
+        const uint32_t* sv = vals;
+        int bits = 8;
+        while (bits < 32 && ((int64_t)1 << bits) < E + 2) bits += 8;
+        bool in_alt = false;
+        rc = radix_sort_pairs<uint32_t>(keys, vals, keys_alt, vals_alt, E, 0, bits, L.sort_ws, &in_alt, st);
+        if (rc) return rc;
+        if (in_alt) { sk = keys_alt; sv = vals_alt; }
+        ptr_etruss_kernel<<<g_e, tb, 0, st>>>(sk, sv, E, L.round_level, ptr_truss, ptr_cap, e_truss, L.ctl,
+                                               stats);
+        TDT_LAUNCH_CHECK("ptr_etruss");
+        stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 0);
+        TDT_LAUNCH_CHECK("stats_final");
+    } else {
+        ktruss_out_kernel<<<g_e, tb, 0, st>>>(L.rnd, E, in_k, L.ctl);
+        TDT_LAUNCH_CHECK("ktruss_out");
+        stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 1);
+        TDT_LAUNCH_CHECK("stats_final");
+    }
+    prof_mark(3, st);
+    return TDT_OK;
+}
+
+}  // namespace tdt

@@ -1,0 +1,136 @@
+"""Whole-path API: truss decomposition, k-truss search and triangle count on
+one GB300, through the C ABI (tdt_truss_decompose / tdt_ktruss_search /
+tdt_triangle_count).
+
+Inputs are the oriented CSRCOO (rows < columns, columns sorted within a row)
+with untiled row offsets; results are keyed by CSR edge position, like the
+reference's e_truss (singlegpu_truss.py:83-101 keeps original positions in
+``edges``).
+"""
+from typing import NamedTuple
+
+import torch
+
+from . import _lib
+
+STAT_STATUS, STAT_KMAX, STAT_NPTR, STAT_ROUNDS, STAT_TRIANGLES, STAT_NETRUSS, STAT_ALIVE = range(7)
+STAT_COUNT = 8
+
+
+class TrussResult(NamedTuple):
+    truss: torch.Tensor       # int32[E]: truss number per edge (2 = in no triangle)
+    e_truss: torch.Tensor     # int32[n]: the reference's peel order (support-0 edges excluded)
+    ptr_truss: torch.Tensor   # int32[kmax-1]: per-level offsets into e_truss
+    kmax: int
+    triangles: int
+    rounds: int
+
+
+class Workspace:
+    """Device scratch reused across calls (grown on demand, torch-allocated)."""
+
+    def __init__(self, device=None):
+        self.device = torch.device(device) if device is not None else torch.device("cuda")
+        self.buf = None
+
+    def get(self, nbytes):
+        if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=self.device)
+        return self.buf
+
+
+_default_ws = {}
+
+
+def _ws_for(device, ws):
+    if ws is not None:
+        return ws
+    key = torch.device(device).index if torch.device(device).index is not None else torch.cuda.current_device()
+    if key not in _default_ws:
+        _default_ws[key] = Workspace(torch.device("cuda", key))
+    return _default_ws[key]
+
+
+def _graph_arrays(graph):
+    cols, rp, rows = graph.columns, graph.row_ptr, graph.rows
+    if not cols.is_cuda:
+        raise TypeError("graph must be on a CUDA device (no CPU path)")
+    if cols.dtype != torch.int32 or not cols.is_contiguous():
+        raise TypeError("columns must be contiguous int32")
+    if rows is not None and (rows.dtype != torch.int32 or not rows.is_contiguous()):
+        raise TypeError("rows must be contiguous int32")
+    if rp.shape[0] < 1:
+        raise ValueError("row_ptr must have V+1 entries")
+    if rp.dtype != torch.int64:
+        rp = rp.to(torch.int64)
+    rp = rp.contiguous()
+    return rows, cols, rp
+
+
+def _check_stats(stats_host, where):
+    st = int(stats_host[STAT_STATUS])
+    if st != 0:
+        raise _lib.TdtError(st, where, "reported by the device")
+
+
+def truss_decompose(graph, workspace=None, stream=None, sync=True):
+    """Full truss decomposition (singlegpu_truss.py:67-158 + :38-45)."""
+    L = _lib.load()
+    rows, cols, rp = _graph_arrays(graph)
+    dev = cols.device
+    V, E = rp.shape[0] - 1, cols.shape[0]
+    truss = torch.empty(E, dtype=torch.int32, device=dev)
+    e_truss = torch.empty(max(E, 1), dtype=torch.int32, device=dev)
+    cap = E + 2
+    ptr = torch.empty(cap, dtype=torch.int32, device=dev)
+    stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
+    need = L.tdt_decompose_workspace_bytes(V, E)
+    ws = _ws_for(dev, workspace).get(need)
+    s = (stream or torch.cuda.current_stream(dev)).cuda_stream
+    rc = L.tdt_truss_decompose(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
+                               truss.data_ptr(), e_truss.data_ptr(), ptr.data_ptr(), cap, stats.data_ptr(),
+                               ws.data_ptr(), ws.numel(), s)
+    _lib.check(rc, "tdt_truss_decompose")
+    if not sync:
+        return truss, e_truss, ptr, stats
+    sh = stats.cpu()
+    _check_stats(sh, "tdt_truss_decompose")
+    return TrussResult(truss, e_truss[: int(sh[STAT_NETRUSS])], ptr[: int(sh[STAT_NPTR])], int(sh[STAT_KMAX]),
+                       int(sh[STAT_TRIANGLES]), int(sh[STAT_ROUNDS]))
+
+
+def ktruss_search(graph, k, workspace=None, stream=None):
+    """Edges of the k-truss (ktruss_search/ktruss_cuda.py:383-463 with l=k-2):
+    returns a bool mask over the CSR edge positions."""
+    L = _lib.load()
+    rows, cols, rp = _graph_arrays(graph)
+    dev = cols.device
+    V, E = rp.shape[0] - 1, cols.shape[0]
+    mask = torch.empty(E, dtype=torch.bool, device=dev)
+    stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
+    ws = _ws_for(dev, workspace).get(L.tdt_decompose_workspace_bytes(V, E))
+    s = (stream or torch.cuda.current_stream(dev)).cuda_stream
+    rc = L.tdt_ktruss_search(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
+                             int(k), mask.data_ptr(), stats.data_ptr(), ws.data_ptr(), ws.numel(), s)
+    _lib.check(rc, "tdt_ktruss_search")
+    _check_stats(stats.cpu(), "tdt_ktruss_search")
+    return mask
+
+
+def triangle_count(graph, workspace=None, stream=None, return_support=False):
+    """Triangle count = sum(support) / 3; optionally the per-edge support."""
+    L = _lib.load()
+    _, cols, rp = _graph_arrays(graph)
+    dev = cols.device
+    V, E = rp.shape[0] - 1, cols.shape[0]
+    support = torch.empty(E, dtype=torch.int32, device=dev) if return_support else None
+    stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
+    ws = _ws_for(dev, workspace).get(L.tdt_decompose_workspace_bytes(V, E))
+    s = (stream or torch.cuda.current_stream(dev)).cuda_stream
+    rc = L.tdt_triangle_count(cols.data_ptr(), rp.data_ptr(), V, E, support.data_ptr() if support is not None else None,
+                              stats.data_ptr(), ws.data_ptr(), ws.numel(), s)
+    _lib.check(rc, "tdt_triangle_count")
+    sh = stats.cpu()
+    _check_stats(sh, "tdt_triangle_count")
+    T = int(sh[STAT_TRIANGLES])
+    return (T, support) if return_support else T

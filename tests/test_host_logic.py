@@ -1,0 +1,67 @@
+"""Host-side logic that needs no GPU: generators, argument checks of the
+drop-in operators, the CSRCOO container."""
+import numpy as np
+import pytest
+import torch
+
+from tdtdecomposition_gb300 import CSRCOO, generators as G, tiling_row_ptr, trusstensor as tt
+from oracle import oracle as O
+
+
+def test_splitmix_stream_is_deterministic():
+    a = G.stream(7, 0, 100)
+    b = G.stream(7, 0, 100)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, G.stream(8, 0, 100))
+    assert np.array_equal(G.stream(7, 50, 50), a[50:])
+
+
+def test_er_has_m_distinct_pairs():
+    s, d = G.er_edges(256, 2000, seed=3)
+    assert len(s) == 2000
+    assert np.all(s < d)
+    assert len(set(zip(s.tolist(), d.tolist()))) == 2000
+
+
+def test_rmat_bits_and_skew():
+    s, d = G.rmat_edges(12, 1 << 15, seed=1)
+    assert s.min() >= 0 and s.max() < 4096 and d.max() < 4096
+    deg = np.bincount(np.concatenate([s, d]), minlength=4096)
+    assert deg.max() > 20 * max(1.0, deg.mean())  # skewed
+
+
+def test_ba_generator_deterministic_and_sized():
+    s, d = G.ba_edges(500, 6, seed=1001)
+    s2, d2 = G.ba_edges(500, 6, seed=1001)
+    assert np.array_equal(s, s2) and np.array_equal(d, d2)
+    assert len(s) == 6 + (500 - 7) * 6
+    rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
+    assert len(cols) == len(s)  # BA draws distinct targets: no duplicates
+
+
+def test_chung_lu_degree_cap():
+    s, d = G.chung_lu_edges(2000, gamma=2.1, mean_degree=10, max_degree=64, seed=2)
+    deg = np.bincount(np.concatenate([s, d]))
+    assert deg.max() < 64 * 1.6
+
+
+def test_tiling_row_ptr_matches_oracle():
+    rows, cols, rp, verts = O.preprocess(np.stack(G.rmat_edges(9, 5000, seed=4), 1))
+    g = CSRCOO.from_numpy(rows, cols, rp)
+    for n_cut in (1, 2, 3):
+        assert np.array_equal(tiling_row_ptr(g, n_cut).numpy(), O.tiling_row_ptr(rows, cols, len(verts), n_cut))
+
+
+def test_operators_reject_cpu_tensors():
+    x = torch.zeros(4, dtype=torch.int32)
+    with pytest.raises(TypeError):
+        tt.segment_add(x, torch.zeros(5, dtype=torch.int32), x)
+    with pytest.raises(TypeError):
+        tt.segment_isin2tile(x, x, torch.zeros(5, dtype=torch.int32), 2, x)
+
+
+def test_out_of_path_operators_raise():
+    with pytest.raises(NotImplementedError):
+        tt.peeling_direct_oo(None)
+    assert len([n for n in tt.__all__ if not n.endswith("_k") and "AffectedSupport" not in n
+                or n.startswith("sub_AllAffected")]) >= 20
