@@ -233,8 +233,9 @@ def main_ours(args):
     barrier(ws)
     launches = L.tdt_launch_count() - n0
     import ctypes
-    ms_s, ms_p, ms_o, nc = ctypes.c_float(), ctypes.c_float(), ctypes.c_float(), ctypes.c_int()
-    L.tdt_profile_stop(ctypes.byref(ms_s), ctypes.byref(ms_p), ctypes.byref(ms_o), ctypes.byref(nc))
+    phases = (ctypes.c_float * 4)()
+    nc = ctypes.c_int()
+    L.tdt_profile_stop(phases, ctypes.byref(nc))
     clk = clocks.stop() if clocks else None
     t_ms = ev0.elapsed_time(ev1)
     t_ms = max_over_ranks(t_ms, ws, dev)
@@ -251,13 +252,16 @@ def main_ours(args):
     d_cols = torch.empty_like(g.columns)
     d_rp = torch.empty_like(g.row_ptr)
 
+    e2e_stats = []
+
     def e2e_step():
         d_rows.copy_(rows_h, non_blocking=True)
         d_cols.copy_(cols_h, non_blocking=True)
         d_rp.copy_(rp_h, non_blocking=True)
-        tr, _, _, _ = T.truss_decompose(CSRCOO(columns=d_cols, row_ptr=d_rp, rows=d_rows), workspace=wsp,
-                                        sync=False)
+        tr, _, _, st = T.truss_decompose(CSRCOO(columns=d_cols, row_ptr=d_rp, rows=d_rows), workspace=wsp,
+                                         sync=False)
         truss_h.copy_(tr, non_blocking=True)
+        e2e_stats.append(st)
 
     e2e_step()
     torch.cuda.synchronize()
@@ -270,7 +274,14 @@ def main_ours(args):
     e1.record(stream)
     torch.cuda.synchronize()
     te = max_over_ranks(e0.elapsed_time(e1), ws, dev)
-    assert torch.equal(truss_h, res.truss.cpu()), "e2e result differs from the resident run"
+    bad = [st.cpu().tolist() for st in e2e_stats if int(st[0]) != 0]
+    ref_truss = res.truss.cpu()
+    if bad or not torch.equal(truss_h, ref_truss):
+        ndiff = int((truss_h != ref_truss).sum())
+        print(json.dumps({"error": "e2e result differs from the resident run", "differing_edges": ndiff,
+                          "bad_stats": bad[:3], "resident_stats": [res.kmax, res.triangles, res.rounds]}),
+              file=sys.stderr, flush=True)
+        raise SystemExit(3)
     e2e_value = ws * E / (te / args.steps / 1e3)
     h2d = rows_h.numel() * 4 + cols_h.numel() * 4 + rp_h.numel() * 8
     d2h = truss_h.numel() * 4
@@ -285,11 +296,12 @@ def main_ours(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     n = max(nc.value, 1)
-    t_sup = ms_s.value / n
-    t_peel = ms_p.value / n
+    t_sup, t_list, t_peel, t_post = (phases[k] / n for k in range(4))
+    # the decomposition's algorithmic bytes B_dec = 2 B_sup: the support pass,
+    # then one re-enumeration of each edge's triangles (listing + peel)
     kernels = {
         "support_kernel": {"ms": t_sup, "bytes": B_sup, "gbs": B_sup / (t_sup / 1e3) / 1e9},
-        "peel_phase": {"ms": t_peel, "bytes": B_sup, "gbs": B_sup / (t_peel / 1e3) / 1e9},
+        "peel_phase": {"ms": t_list + t_peel, "bytes": B_sup, "gbs": B_sup / ((t_list + t_peel) / 1e3) / 1e9},
     }
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     traffic = None
@@ -305,7 +317,8 @@ def main_ours(args):
             "traffic": traffic, "peak_source": peak_src,
             "per_kernel": {k: {"ms": round(v["ms"], 4), "achieved_gbs": round(v["gbs"], 1),
                                "algorithmic_bytes": v["bytes"]} for k, v in kernels.items()},
-            "post_phase_ms": ms_o.value / n}
+            "phase_ms": {"support": t_sup, "listing": t_list, "peel": t_peel, "outputs": t_post},
+            "decomposition_gbs_of_2Bsup": 2 * B_sup / (ms_step / 1e3) / 1e9}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",

@@ -54,11 +54,19 @@ unsigned long long tdt_launch_count(void);
 
 /* Phase timing of the whole-path calls: after tdt_profile_start(n), the next
  * n calls record CUDA events on their stream; tdt_profile_stop() waits for
- * them and returns the summed milliseconds of the support kernel, of the
- * peel phase (in-adjacency build, state init and the persistent peel kernel)
- * and of the output phase, with the number of calls recorded (host pointers). */
+ * them and writes the summed milliseconds of four phases to ms_phase[4]
+ * (host): [0] the support pass, [1] the triangle-listing pass, [2] the peel
+ * (in-adjacency build and the persistent peel kernel), [3] the outputs; and
+ * the number of calls recorded to *ncalls. */
 int tdt_profile_start(int max_calls);
-int tdt_profile_stop(float *ms_support, float *ms_peel, float *ms_post, int *ncalls);
+int tdt_profile_stop(float *ms_phase, int *ncalls);
+
+/* Testing knob of the support/listing kernels: rows with out-degree <=
+ * warp_cap are processed by one warp, heavier rows by a block with the row
+ * staged in shared memory up to heavy_cap entries, and beyond that in place.
+ * Lower values let small graphs exercise every path; 0 restores the
+ * defaults.  Affects calls launched afterwards from any thread. */
+void tdt_set_support_caps(int warp_cap, int heavy_cap);
 
 /* =====================================================================
  * Drop-in `trusstensor` operators.
@@ -190,7 +198,11 @@ enum tdt_stat_index {
     TDT_STAT_COUNT = 8
 };
 
-/* Workspace for tdt_truss_decompose / tdt_ktruss_search / tdt_triangle_count. */
+/* Workspace for tdt_truss_decompose / tdt_ktruss_search / tdt_triangle_count.
+ * Workspace bytes beyond this size (rounded up to 256) hold per-edge triangle
+ * lists: when 24 * T bytes fit there (T = triangle count), the peel reads each
+ * peeled edge's triangles from its list; otherwise it finds them by binary
+ * search in the adjacency.  Results are identical either way. */
 size_t tdt_decompose_workspace_bytes(int64_t num_vertices, int64_t num_edges);
 
 /* Full truss decomposition: the single-call replacement of the `--cuda` flow

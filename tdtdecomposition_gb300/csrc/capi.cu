@@ -13,13 +13,15 @@ static unsigned long long g_launches = 0;
 void note_launch() { __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED); }
 
 // Phase timing of the whole-path calls (CUDA events on the launching stream).
+constexpr int kPhases = 5;
 struct PhaseRec {
-    cudaEvent_t ev[4];
+    cudaEvent_t ev[kPhases];
 };
 static PhaseRec* g_prof = nullptr;
 static int g_prof_cap = 0, g_prof_n = 0, g_prof_on = 0;
 
-// Called by run_peel: phase 0 = start, 1 = after support, 2 = after peel, 3 = end.
+// Called by run_peel: phase 0 = start, 1 = after the support pass, 2 = after
+// the listing pass, 3 = after the peel, 4 = end.
 void prof_mark(int phase, cudaStream_t st) {
     if (!g_prof_on) return;
     if (phase == 0) {
@@ -79,15 +81,15 @@ int launch_support_k(const int32_t*, const int32_t*, const int32_t*, int64_t, in
                      cudaStream_t);
 int launch_sub_affect(const int32_t*, const int32_t*, const int32_t*, int64_t, int32_t, const uint8_t*, int32_t*,
                       int64_t, cudaStream_t);
-// support.cu
-template <bool kIdOrdered, class Off>
-int launch_support(const Off* rp, int32_t stride, const int32_t* cols, int64_t nv, int64_t ne, int32_t* out,
-                   void* ctl_ws, const int* gate, cudaStream_t st);
 // peel.cu
 size_t decompose_workspace_bytes(int64_t V, int64_t E);
 int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* rp, int64_t V, int64_t E,
              int32_t fixed_level, int32_t* truss, int32_t* e_truss, int32_t* ptr_truss, int64_t ptr_cap,
              uint8_t* in_k, int32_t* support_out, int64_t* stats, void* ws, size_t ws_bytes, cudaStream_t st);
+
+void set_support_caps(int warp_cap, int heavy_cap);
+int launch_support_accum_i32(const int32_t* rp, int32_t stride, const int32_t* cols, int64_t nv, int64_t ne,
+                             int32_t* out, cudaStream_t st);
 
 // The drop-in support op takes no workspace (as in the reference), so it runs
 // the support kernel with its scratch-free static schedule.
@@ -99,8 +101,7 @@ static int op_support(const int32_t* a_rows, const int32_t* cols, const int32_t*
     TDT_CHECK_ARG(n_edges >= 0, "negative size");
     if (n_edges == 0) return TDT_OK;
     TDT_CHECK_ARG(a_rows && cols && rp && out, "null pointer");
-    return launch_support<false, int32_t>(rp, n_cut, cols, (rp_len - 1) / n_cut, n_edges, out, nullptr, nullptr,
-                                          st);
+    return launch_support_accum_i32(rp, n_cut, cols, (rp_len - 1) / n_cut, n_edges, out, st);
 }
 
 }  // namespace tdt
@@ -125,15 +126,17 @@ API const char* tdt_status_string(int s) {
 API const char* tdt_last_error(void) { return g_err; }
 API unsigned long long tdt_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
+API void tdt_set_support_caps(int warp_cap, int heavy_cap) { set_support_caps(warp_cap, heavy_cap); }
+
 API int tdt_profile_start(int max_calls) {
     TDT_CHECK_ARG(max_calls > 0 && max_calls <= 4096, "max_calls out of range");
     if (g_prof_cap < max_calls) {
         PhaseRec* p = new PhaseRec[max_calls];
         for (int i = 0; i < max_calls; i++)
-            for (int k = 0; k < 4; k++) TDT_CUDA(cudaEventCreate(&p[i].ev[k]));
+            for (int k = 0; k < kPhases; k++) TDT_CUDA(cudaEventCreate(&p[i].ev[k]));
         if (g_prof) {
             for (int i = 0; i < g_prof_cap; i++)
-                for (int k = 0; k < 4; k++) cudaEventDestroy(g_prof[i].ev[k]);
+                for (int k = 0; k < kPhases; k++) cudaEventDestroy(g_prof[i].ev[k]);
             delete[] g_prof;
         }
         g_prof = p;
@@ -144,19 +147,19 @@ API int tdt_profile_start(int max_calls) {
     return TDT_OK;
 }
 
-API int tdt_profile_stop(float* ms_support, float* ms_peel, float* ms_post, int* ncalls) {
+API int tdt_profile_stop(float* ms_phase, int* ncalls) {
     g_prof_on = 0;
-    float a = 0, b = 0, c = 0;
+    float acc[kPhases - 1] = {0, 0, 0, 0};
     for (int i = 0; i < g_prof_n; i++) {
-        TDT_CUDA(cudaEventSynchronize(g_prof[i].ev[3]));
-        float x;
-        TDT_CUDA(cudaEventElapsedTime(&x, g_prof[i].ev[0], g_prof[i].ev[1])); a += x;
-        TDT_CUDA(cudaEventElapsedTime(&x, g_prof[i].ev[1], g_prof[i].ev[2])); b += x;
-        TDT_CUDA(cudaEventElapsedTime(&x, g_prof[i].ev[2], g_prof[i].ev[3])); c += x;
+        TDT_CUDA(cudaEventSynchronize(g_prof[i].ev[kPhases - 1]));
+        for (int k = 0; k + 1 < kPhases; k++) {
+            float x;
+            TDT_CUDA(cudaEventElapsedTime(&x, g_prof[i].ev[k], g_prof[i].ev[k + 1]));
+            acc[k] += x;
+        }
     }
-    if (ms_support) *ms_support = a;
-    if (ms_peel) *ms_peel = b;
-    if (ms_post) *ms_post = c;
+    if (ms_phase)
+        for (int k = 0; k + 1 < kPhases; k++) ms_phase[k] = acc[k];
     if (ncalls) *ncalls = g_prof_n;
     return TDT_OK;
 }

@@ -49,7 +49,9 @@ struct PeelCtl {
     unsigned long long q[3];      // packed (items << kCandBits | candidates) per round slot
     unsigned long long fe[3];     // frontier edges per round slot (queued or not)
     int min_sup[2];
-    int level;
+    int listed;                   // 1: per-edge triangle lists were built (they fit the workspace)
+    int list_skip;                // gate of the listing pass and of the list-only setup kernels
+    int enum_skip;                // gate of the in-adjacency build (needed without lists)
     int pad0;
     long long rounds;
     long long triangles;
@@ -68,6 +70,8 @@ struct PeelArgs {
     int32_t* round_level;
     int4* qi[2];
     long long* qb[2];
+    const int64_t* off;   // listed mode: list offsets int64[E+1]
+    const int2* lists;    // listed mode: partner edge pairs
     int64_t V, E, round_cap;
     int32_t mode;         // 0: full decomposition, 1: fixed-level peel (k-truss search)
     int32_t fixed_level;
@@ -94,7 +98,10 @@ __device__ __forceinline__ void warp_append(const PeelArgs& A, int slot, int buf
     int32_t x = 0, y = 0, dxo = 0;
     long long dx = 0;
     bool q = want && cur_sup > 0;
-    if (q) {
+    if (q && A.lists) {
+        dx = __ldg(A.off + e + 1) - __ldg(A.off + e);  // the edge's original triangles
+        if (dx <= 0) q = false;
+    } else if (q) {
         const int32_t u = __ldg(A.rows + e), v = __ldg(A.cols + e);
         const long long duo = __ldg(A.rp + u + 1) - __ldg(A.rp + u);
         const long long du = duo + __ldg(A.cp + u + 1) - __ldg(A.cp + u);
@@ -202,6 +209,7 @@ __device__ bool fixed_start(const PeelArgs& A, int32_t l) {
 
 __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
     __shared__ long long s_win[kPeelWarps][kWarp];
+    if (!*(volatile int*)&A.ctl->listed) A.lists = nullptr;
     const unsigned lane = lane_id();
     const int wib = threadIdx.x / kWarp;
     const int64_t gwarp = (int64_t)blockIdx.x * kPeelWarps + wib;
@@ -238,35 +246,61 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
         const long long T = (long long)(packed & kCandMask);
         const long long* __restrict__ qb = A.qb[buf];
         const int4* __restrict__ qi = A.qi[buf];
-        for (long long cb = gwarp * kWarp; cb < T; cb += nwarps * kWarp) {
-            // item owning slot cb: last i with qb[i] <= cb
-            long long i0 = 0;
+        // each warp owns a contiguous range of candidate slots; the owning item
+        // of its first slot is found once, later ones by sliding the window
+        const long long per_warp = (((T + nwarps - 1) / nwarps) + 31) & ~31ll;
+        const long long cb0 = gwarp * per_warp;
+        const long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
+        long long i0 = 0;
+        if (cb0 < cb1) {
             if (lane == 0) {
                 long long lo = 0, hi = N - 1;
                 while (lo < hi) {
                     long long mid = (lo + hi + 1) >> 1;
-                    if (__ldcg(qb + mid) <= cb) lo = mid; else hi = mid - 1;
+                    if (__ldcg(qb + mid) <= cb0) lo = mid; else hi = mid - 1;
                 }
                 i0 = lo;
             }
             i0 = __shfl_sync(kFull, i0, 0);
+        }
+        for (long long cb = cb0; cb < cb1; cb += kWarp) {
             s_win[wib][lane] = (i0 + lane < N) ? __ldcg(qb + i0 + lane) : LLONG_MAX;
             __syncwarp();
             const long long t = cb + lane;
             bool want_f = false, want_g = false;
             int64_t f = 0, g = 0;
-            if (t < T) {
+            // window index of this lane's item: slot cb lies in item i0 and each
+            // item owns >= 1 slot, so slot cb+k lies in item i0+k at most; the
+            // window holds i0..i0+31, and i0+32 is checked with one more load
+            int jl = 0;
+            long long base_l = 0;
+            {
                 int lo = 0, hi = 31;
                 while (lo < hi) {
                     int mid = (lo + hi + 1) >> 1;
                     if (s_win[wib][mid] <= t) lo = mid; else hi = mid - 1;
                 }
+                jl = lo;
+                base_l = s_win[wib][lo];
+                if (lo == 31 && i0 + 32 < N) {
+                    const long long nb = __ldcg(qb + i0 + 32);
+                    if (nb <= t) { jl = 32; base_l = nb; }
+                }
+            }
+            if (t < cb1) {
+                const int lo = jl;
                 const long long item = i0 + lo;
                 const int4 it = __ldcg(qi + item);
                 const int32_t e = it.x, x = it.y, y = it.z, dxo = it.w;
-                const long long tl = t - s_win[wib][lo];
-                int32_t w;
-                if (tl < dxo) {
+                const long long tl = t - base_l;
+                int32_t w = y;
+                if (A.lists) {
+                    // listed mode: the slot is one of e's triangles, (f, g) its other edges
+                    const int2 fg = __ldg(A.lists + __ldg(A.off + e) + tl);
+                    f = fg.x;
+                    g = fg.y;
+                    w = ~y;  // any value != y
+                } else if (tl < dxo) {
                     f = __ldg(A.rp + x) + tl;
                     w = __ldg(A.cols + f);
                 } else {
@@ -275,8 +309,9 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
                     f = __ldg(A.in_eid + k);
                 }
                 if (w != y) {
-                    g = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
-                                : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
+                    if (!A.lists)
+                        g = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
+                                    : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
                     if (g >= 0) {
                         const int32_t rf = __ldcg(A.rnd + f), rg = __ldcg(A.rnd + g);
                         const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
@@ -296,6 +331,21 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
             }
             warp_append(A, nslot, nbuf, want_f, (int32_t)f, l);
             warp_append(A, nslot, nbuf, want_g, (int32_t)g, l);
+            {
+                // the next window starts at the item of slot cb+32 (<= i0+32)
+                int jn = 0;
+                if (lane == 31) {
+                    const long long tn = cb + kWarp;
+                    int lo = 0, hi = 31;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (s_win[wib][mid] <= tn) lo = mid; else hi = mid - 1;
+                    }
+                    jn = lo;
+                    if (lo == 31 && i0 + 32 < N && __ldcg(qb + i0 + 32) <= tn) jn = 32;
+                }
+                i0 += __shfl_sync(kFull, jn, 31);
+            }
             __syncwarp();
         }
         if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
@@ -352,7 +402,7 @@ __global__ void validate_kernel(const int64_t* __restrict__ rp, const int32_t* _
 
 __global__ void indeg_kernel(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t E,
                              int64_t V, int32_t* __restrict__ indeg, const PeelCtl* ctl) {
-    if (*(volatile const int*)&ctl->g.status != 0) return;
+    if (*(volatile const int*)&ctl->g.status != 0 || *(volatile const int*)&ctl->enum_skip) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x)
         atomicAdd(indeg + cols[e], 1);
@@ -361,7 +411,7 @@ __global__ void indeg_kernel(const int32_t* __restrict__ rows, const int32_t* __
 __global__ void csc_fill_kernel(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t E,
                                 int64_t V, const int64_t* __restrict__ cp, int32_t* __restrict__ cursor,
                                 int32_t* __restrict__ in_src, int32_t* __restrict__ in_eid, const PeelCtl* ctl) {
-    if (*(volatile const int*)&ctl->g.status != 0) return;
+    if (*(volatile const int*)&ctl->g.status != 0 || *(volatile const int*)&ctl->enum_skip) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t u = rows[e], v = cols[e];
@@ -371,8 +421,11 @@ __global__ void csc_fill_kernel(const int32_t* __restrict__ rows, const int32_t*
     }
 }
 
-__global__ void init_state_kernel(const int32_t* __restrict__ sup, int32_t* __restrict__ rnd, int64_t E,
-                                  PeelCtl* ctl) {
+// sup = cA + cB + cC (the role counts of the support pass), rnd = alive,
+// triangle total.
+__global__ void init_state_kernel(const int32_t* __restrict__ cA, const int32_t* __restrict__ cB,
+                                  const int32_t* __restrict__ cC, int32_t* __restrict__ sup,
+                                  int32_t* __restrict__ rnd, int64_t E, PeelCtl* ctl) {
     __shared__ long long s_part[32];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctl->min_sup[0] = INT32_MAX;
@@ -381,8 +434,10 @@ __global__ void init_state_kernel(const int32_t* __restrict__ sup, int32_t* __re
     long long acc = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t s = cA[e] + cB[e] + cC[e];
+        sup[e] = s;
         rnd[e] = -1;
-        acc += sup[e];
+        acc += s;
     }
     acc = warp_sum(acc);
     if (lane_id() == 0) s_part[threadIdx.x / kWarp] = acc;
@@ -391,6 +446,48 @@ __global__ void init_state_kernel(const int32_t* __restrict__ sup, int32_t* __re
         long long b = 0;
         for (int i = 0; i < (int)(blockDim.x / kWarp); i++) b += s_part[i];
         atomicAdd((unsigned long long*)&ctl->triangles, (unsigned long long)b);
+    }
+}
+
+// Lists fit when 8 bytes x (3T = off[E]) fit the workspace tail.
+__global__ void list_decide_kernel(const int64_t* __restrict__ off, int64_t E, unsigned long long tail_bytes,
+                                   int want_lists, PeelCtl* ctl) {
+    const unsigned long long need = 8ull * (unsigned long long)off[E];
+    const int ok = want_lists && ctl->g.status == 0 && need <= tail_bytes;
+    ctl->listed = ok;
+    ctl->list_skip = !ok;
+    ctl->enum_skip = ok;
+}
+
+// Slot cursors of the listing pass: role A at off[e], role B at off[e] + cA[e],
+// role C at off[e] + cA[e] + cB[e].
+__global__ void list_cursor_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ cA,
+                                   const int32_t* __restrict__ cB, int64_t E, unsigned long long* __restrict__ curA,
+                                   unsigned long long* __restrict__ curB, unsigned long long* __restrict__ curC,
+                                   const PeelCtl* ctl) {
+    if (*(volatile const int*)&ctl->list_skip) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long o = (unsigned long long)off[e];
+        curA[e] = o;
+        curB[e] = o + cA[e];
+        curC[e] = o + cA[e] + cB[e];
+    }
+}
+
+// After the listing pass every role-C cursor must sit at the end of its
+// edge's list (and every role-B cursor of rows listed in place at the start
+// of role C); anything else means the two passes disagreed.
+__global__ void list_check_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ cA,
+                                  const int32_t* __restrict__ cB, int64_t E,
+                                  const unsigned long long* __restrict__ curB,
+                                  const unsigned long long* __restrict__ curC, PeelCtl* ctl) {
+    if (*(volatile const int*)&ctl->list_skip) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        if (curC[e] != (unsigned long long)off[e + 1]) atomicMax(&ctl->g.status, (int)TDT_ERR_CAPACITY);
+        const unsigned long long b0 = (unsigned long long)off[e] + cA[e];
+        if (curB[e] != b0 && curB[e] != b0 + cB[e]) atomicMax(&ctl->g.status, (int)TDT_ERR_CAPACITY);
     }
 }
 
@@ -483,8 +580,12 @@ __global__ void stats_final_kernel(PeelCtl* ctl, int64_t* stats, int mode) {
 
 // ------------------------------------------------------------------ host side
 void prof_mark(int phase, cudaStream_t st);
-int launch_support_i64(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* out, void* ctl,
-                       const int* gate, cudaStream_t st);
+int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* cA, int32_t* cB,
+                         int32_t* cC, void* ctl, const int* gate, cudaStream_t st);
+int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* off,
+                        const int32_t* cA, const int32_t* cB, unsigned long long* curA_g,
+                        unsigned long long* curB_g, unsigned long long* curC, int2* lists, void* ctl,
+                        const int* gate, int* status, cudaStream_t st);
 
 namespace {
 struct Carver {
@@ -512,6 +613,7 @@ struct Layout {
     int32_t* round_level;
     int4* qi[2];
     long long* qb[2];
+    int64_t* off;
     void* scan_ws;
     void* sort_ws;
     size_t total;
@@ -535,7 +637,8 @@ Layout carve(void* ws, int64_t V, int64_t E) {
         L.qi[b] = (int4*)c.take(16 * e);
         L.qb[b] = (long long*)c.take(8 * e);
     }
-    size_t scan_b = scan_scratch_bytes((int64_t)v + 1);
+    L.off = (int64_t*)c.take(8 * (e + 1));
+    size_t scan_b = scan_scratch_bytes((int64_t)(e > v ? e : v) + 1);
     L.scan_ws = c.take(scan_b);
     L.sort_ws = c.take(radix_sort_scratch_bytes((int64_t)e));
     L.total = c.off + 256;
@@ -588,23 +691,44 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     }
     validate_kernel<<<g_e, tb, 0, st>>>(rp, rows_use, cols, E, V, L.ctl);
     TDT_LAUNCH_CHECK("validate");
-    // support (skipped on the device when validation failed)
-    TDT_CUDA(cudaMemsetAsync(L.sup, 0, 4 * (size_t)E, st));
+    // pass 1: support role counts (skipped on the device when validation failed);
+    // cA, cB, cC live in the first queue buffer until the peel starts
+    int32_t* cA = reinterpret_cast<int32_t*>(L.qi[0]);
+    int32_t* cB = cA + E;
+    int32_t* cC = cB + E;
     prof_mark(0, st);
-    rc = launch_support_i64(rp, cols, V, E, L.sup, L.sup_ctl, &L.ctl->g.status, st);
+    rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->g.status, st);
     if (rc) return rc;
+    init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.rnd, E, L.ctl);
+    TDT_LAUNCH_CHECK("init_state");
     prof_mark(1, st);
     if (mode == 2) {
-        init_state_kernel<<<g_e, tb, 0, st>>>(L.sup, L.rnd, E, L.ctl);
-        TDT_LAUNCH_CHECK("init_state");
         if (support_out) TDT_CUDA(cudaMemcpyAsync(support_out, L.sup, 4 * (size_t)E, cudaMemcpyDeviceToDevice, st));
         stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 1);
         TDT_LAUNCH_CHECK("stats_final");
-        prof_mark(2, st);
-        prof_mark(3, st);
+        for (int ph = 2; ph <= 4; ph++) prof_mark(ph, st);
         return TDT_OK;
     }
-    // in-adjacency (CSC) of the oriented graph
+    // pass 2: per-edge triangle lists in the workspace tail when 24 T bytes fit
+    rc = exclusive_scan<int32_t, int64_t>(L.sup, L.off, E, L.off + E, L.scan_ws, st);
+    if (rc) return rc;
+    const size_t list_base = (need + 255) & ~(size_t)255;
+    const unsigned long long tail = ws_bytes > list_base ? (unsigned long long)(ws_bytes - list_base) : 0ull;
+    int2* lists = reinterpret_cast<int2*>(reinterpret_cast<char*>(ws) + list_base);
+    list_decide_kernel<<<1, 1, 0, st>>>(L.off, E, tail, tail > 0, L.ctl);
+    TDT_LAUNCH_CHECK("list_decide");
+    unsigned long long* curC = reinterpret_cast<unsigned long long*>(L.qi[1]);
+    unsigned long long* curA = reinterpret_cast<unsigned long long*>(L.qb[0]);
+    unsigned long long* curB = reinterpret_cast<unsigned long long*>(L.qb[1]);
+    list_cursor_kernel<<<g_e, tb, 0, st>>>(L.off, cA, cB, E, curA, curB, curC, L.ctl);
+    TDT_LAUNCH_CHECK("list_cursor");
+    rc = launch_support_list(rp, cols, V, E, L.off, cA, cB, curA, curB, curC, lists, L.sup_ctl, &L.ctl->list_skip,
+                             &L.ctl->g.status, st);
+    if (rc) return rc;
+    list_check_kernel<<<g_e, tb, 0, st>>>(L.off, cA, cB, E, curB, curC, L.ctl);
+    TDT_LAUNCH_CHECK("list_check");
+    prof_mark(2, st);
+    // in-adjacency (CSC) of the oriented graph, for the peel without lists
     TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
     indeg_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.indeg, L.ctl);
     TDT_LAUNCH_CHECK("indeg");
@@ -613,8 +737,6 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
     csc_fill_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.cp, L.indeg, L.in_src, L.in_eid, L.ctl);
     TDT_LAUNCH_CHECK("csc_fill");
-    init_state_kernel<<<g_e, tb, 0, st>>>(L.sup, L.rnd, E, L.ctl);
-    TDT_LAUNCH_CHECK("init_state");
 
     // persistent peel
     int occ = 0;
@@ -627,16 +749,16 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     A.rp = rp; A.cols = cols; A.rows = rows_use; A.cp = L.cp; A.in_src = L.in_src; A.in_eid = L.in_eid;
     A.sup = L.sup; A.rnd = L.rnd; A.round_level = L.round_level;
     A.qi[0] = L.qi[0]; A.qi[1] = L.qi[1]; A.qb[0] = L.qb[0]; A.qb[1] = L.qb[1];
+    A.off = L.off; A.lists = lists;
     A.V = V; A.E = E; A.round_cap = E + 2;
     A.mode = mode == 0 ? 0 : 1;
     A.fixed_level = fixed_level;
     A.ctl = L.ctl;
     dim3 grid(di.sms * occ), block(kPeelBlock);
     void* args[] = {&A};
-    // the peel phase also covers the CSC build and state init launched above
     TDT_CUDA(cudaLaunchCooperativeKernel((void*)peel_kernel, grid, block, args, 0, st));
     note_launch();
-    prof_mark(2, st);
+    prof_mark(3, st);
 
     if (mode == 0) {
         // outputs: truss numbers, then e_truss / ptr_truss from a stable sort by round
@@ -665,7 +787,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
         stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 1);
         TDT_LAUNCH_CHECK("stats_final");
     }
-    prof_mark(3, st);
+    prof_mark(4, st);
     return TDT_OK;
 }
 

@@ -27,16 +27,46 @@ class TrussResult(NamedTuple):
 
 
 class Workspace:
-    """Device scratch reused across calls (grown on demand, torch-allocated)."""
+    """Device scratch reused across calls (grown on demand, torch-allocated).
+
+    It also remembers the triangle count of the graphs it has served, so that
+    later calls on the same graph can size the per-edge triangle lists."""
 
     def __init__(self, device=None):
         self.device = torch.device(device) if device is not None else torch.device("cuda")
         self.buf = None
+        self.triangles = {}
 
     def get(self, nbytes):
         if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = None
             self.buf = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=self.device)
         return self.buf
+
+
+def _graph_key(cols, rp):
+    return (cols.data_ptr(), cols.shape[0], rp.shape[0])
+
+
+LIST_BUDGET_FRACTION = 0.6
+
+
+def _list_bytes(ws, cols, rp, lists, base):
+    """Bytes for the per-edge triangle lists (24 per triangle), or 0 to let
+    the peel search the adjacency instead.  lists: True/False/"auto"."""
+    if lists is False:
+        return 0
+    key = _graph_key(cols, rp)
+    T = ws.triangles.get(key)
+    if T is None:
+        T = triangle_count_arrays(cols, rp, ws)
+        ws.triangles[key] = T
+    need = 24 * T + 256
+    if lists is True:
+        return need
+    free, _ = torch.cuda.mem_get_info(cols.device)
+    have = free + (ws.buf.numel() if ws.buf is not None else 0) - base
+    return need if need <= LIST_BUDGET_FRACTION * have else 0
 
 
 _default_ws = {}
@@ -73,8 +103,12 @@ def _check_stats(stats_host, where):
         raise _lib.TdtError(st, where, "reported by the device")
 
 
-def truss_decompose(graph, workspace=None, stream=None, sync=True):
-    """Full truss decomposition (singlegpu_truss.py:67-158 + :38-45)."""
+def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto"):
+    """Full truss decomposition (singlegpu_truss.py:67-158 + :38-45).
+
+    lists: "auto" keeps per-edge triangle lists in the workspace when they fit
+    in LIST_BUDGET_FRACTION of the free device memory (the first call on a
+    graph then counts its triangles first), True always, False never."""
     L = _lib.load()
     rows, cols, rp = _graph_arrays(graph)
     dev = cols.device
@@ -85,7 +119,9 @@ def truss_decompose(graph, workspace=None, stream=None, sync=True):
     ptr = torch.empty(cap, dtype=torch.int32, device=dev)
     stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
     need = L.tdt_decompose_workspace_bytes(V, E)
-    ws = _ws_for(dev, workspace).get(need)
+    wso = _ws_for(dev, workspace)
+    base = (need + 255) // 256 * 256
+    ws = wso.get(base + _list_bytes(wso, cols, rp, lists, base))
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
     rc = L.tdt_truss_decompose(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
                                truss.data_ptr(), e_truss.data_ptr(), ptr.data_ptr(), cap, stats.data_ptr(),
@@ -99,7 +135,7 @@ def truss_decompose(graph, workspace=None, stream=None, sync=True):
                        int(sh[STAT_TRIANGLES]), int(sh[STAT_ROUNDS]))
 
 
-def ktruss_search(graph, k, workspace=None, stream=None):
+def ktruss_search(graph, k, workspace=None, stream=None, lists="auto"):
     """Edges of the k-truss (ktruss_search/ktruss_cuda.py:383-463 with l=k-2):
     returns a bool mask over the CSR edge positions."""
     L = _lib.load()
@@ -108,13 +144,28 @@ def ktruss_search(graph, k, workspace=None, stream=None):
     V, E = rp.shape[0] - 1, cols.shape[0]
     mask = torch.empty(E, dtype=torch.bool, device=dev)
     stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
-    ws = _ws_for(dev, workspace).get(L.tdt_decompose_workspace_bytes(V, E))
+    wso = _ws_for(dev, workspace)
+    base = (L.tdt_decompose_workspace_bytes(V, E) + 255) // 256 * 256
+    ws = wso.get(base + _list_bytes(wso, cols, rp, lists, base))
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
     rc = L.tdt_ktruss_search(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
                              int(k), mask.data_ptr(), stats.data_ptr(), ws.data_ptr(), ws.numel(), s)
     _lib.check(rc, "tdt_ktruss_search")
     _check_stats(stats.cpu(), "tdt_ktruss_search")
     return mask
+
+
+def triangle_count_arrays(cols, rp, ws):
+    L = _lib.load()
+    V, E = rp.shape[0] - 1, cols.shape[0]
+    stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=cols.device)
+    buf = ws.get(L.tdt_decompose_workspace_bytes(V, E))
+    rc = L.tdt_triangle_count(cols.data_ptr(), rp.data_ptr(), V, E, None, stats.data_ptr(), buf.data_ptr(),
+                              buf.numel(), torch.cuda.current_stream(cols.device).cuda_stream)
+    _lib.check(rc, "tdt_triangle_count")
+    sh = stats.cpu()
+    _check_stats(sh, "tdt_triangle_count")
+    return int(sh[STAT_TRIANGLES])
 
 
 def triangle_count(graph, workspace=None, stream=None, return_support=False):

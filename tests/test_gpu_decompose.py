@@ -20,10 +20,12 @@ def graph_of(rows, cols, rp):
 
 
 @pytest.mark.parametrize("name", CASES)
-def test_decompose_matches_reference_peel_order(name):
+@pytest.mark.parametrize("lists", [True, False])
+def test_decompose_matches_reference_peel_order(name, lists):
+    """Both peel modes: triangles read from per-edge lists, or found by search."""
     d = GD.load(name)
     g = graph_of(d["ref_rows"], d["ref_cols"], d["ref_rp"])
-    res = T.truss_decompose(g)
+    res = T.truss_decompose(g, lists=lists)
     assert res.kmax == int(d["sg_kmax2"]) == int(d["sg_kmax1"])
     assert np.array_equal(res.e_truss.cpu().numpy(), d["sg_e_truss2"])
     assert np.array_equal(res.e_truss.cpu().numpy(), d["sg_e_truss1"])
@@ -43,12 +45,13 @@ def test_decompose_without_rows(name):
 
 
 @pytest.mark.parametrize("name", CASES)
-def test_ktruss_search_matches_reference(name):
+@pytest.mark.parametrize("lists", [True, False])
+def test_ktruss_search_matches_reference(name, lists):
     d = GD.load(name)
     g = graph_of(d["ref_rows"], d["ref_cols"], d["ref_rp"])
     truss = GD.truss_from_levels(d["sg_e_truss2"], d["sg_ptr_truss2"], d["ref_cols"].shape[0])
     for k in list(d["kt_ks"]) + [1, 2]:
-        m = T.ktruss_search(g, int(k)).cpu().numpy()
+        m = T.ktruss_search(g, int(k), lists=lists).cpu().numpy()
         assert np.array_equal(m, truss >= k), k
         if ("kt_rows_k%d" % k) in d:
             got = GD.edge_set(d["ref_rows"][m], d["ref_cols"][m])
@@ -68,11 +71,13 @@ def _oracle_check(pairs, n_cut=2):
     rows, cols, rp, verts = O.preprocess(pairs, stable=True)
     V = len(verts)
     kmax, et, pt, truss = O.k_truss(rows, cols, O.tiling_row_ptr(rows, cols, V, n_cut), V, n_cut)
-    res = T.truss_decompose(graph_of(rows, cols, rp))
-    assert res.kmax == kmax
-    assert np.array_equal(res.ptr_truss.cpu().numpy(), pt)
-    assert np.array_equal(res.e_truss.cpu().numpy(), et)
-    assert np.array_equal(res.truss.cpu().numpy(), truss)
+    g = graph_of(rows, cols, rp)
+    for lists in (True, False):
+        res = T.truss_decompose(g, lists=lists)
+        assert res.kmax == kmax
+        assert np.array_equal(res.ptr_truss.cpu().numpy(), pt)
+        assert np.array_equal(res.e_truss.cpu().numpy(), et)
+        assert np.array_equal(res.truss.cpu().numpy(), truss)
     return res
 
 
@@ -126,6 +131,24 @@ def test_rejects_unoriented_graph():
         T.truss_decompose(graph_of(rows, cols, rp))
 
 
+def test_list_capacity_fallback():
+    """A workspace tail too small for the lists falls back to the search peel
+    on the device, with identical results."""
+    from tdtdecomposition_gb300 import _lib
+    s, d = G.rmat_edges(12, 16 << 12, seed=3)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
+    g = graph_of(rows, cols, rp)
+    full = T.truss_decompose(g, lists=True)
+    L = _lib.load()
+    V, E = len(verts), len(cols)
+    base = (L.tdt_decompose_workspace_bytes(V, E) + 255) // 256 * 256
+    ws = T.Workspace()
+    ws.buf = torch.empty(base + 1024, dtype=torch.uint8, device="cuda")  # tail of 1 KB: too small
+    ws.triangles[T._graph_key(g.columns, g.row_ptr.long())] = 1
+    small = T.truss_decompose(g, workspace=ws, lists=True)
+    assert torch.equal(full.truss, small.truss) and torch.equal(full.e_truss, small.e_truss)
+
+
 def test_repeatable_and_workspace_reuse():
     s, d = G.rmat_edges(13, 16 << 13, seed=21)
     rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
@@ -133,4 +156,76 @@ def test_repeatable_and_workspace_reuse():
     ws = T.Workspace()
     a = T.truss_decompose(g, workspace=ws)
     b = T.truss_decompose(g, workspace=ws)
+    assert torch.equal(a.truss, b.truss) and torch.equal(a.e_truss, b.e_truss)
+
+
+@pytest.mark.parametrize("caps", [(4, 16), (8, 10 ** 6), (2, 3)])
+def test_all_support_paths_vs_oracle(caps):
+    """Lowered light/heavy thresholds push small graphs through the block-level
+    heavy-row walk and the in-place (beyond shared memory) path."""
+    from tdtdecomposition_gb300 import _lib
+    L = _lib.load()
+    s, d = G.rmat_edges(12, 16 << 12, seed=31)
+    pairs = np.stack([s, d], 1)
+    rows, cols, rp, verts = O.preprocess(pairs)
+    sup_ref = O.support(rows, cols, rp.astype(np.int32), 1)
+    L.tdt_set_support_caps(*caps)
+    try:
+        t, sup = T.triangle_count(graph_of(rows, cols, rp), return_support=True)
+        assert np.array_equal(sup.cpu().numpy(), sup_ref)
+        _oracle_check(pairs)
+        # the drop-in operator (accumulate mode, int32 offsets, any orientation)
+        from tdtdecomposition_gb300 import trusstensor as tt
+        out = torch.zeros(len(cols), dtype=torch.int32, device="cuda")
+        tt.segment_isin2(torch.as_tensor(rows).cuda(), torch.as_tensor(cols).cuda(),
+                         torch.as_tensor(rp.astype(np.int32)).cuda(), out)
+        assert np.array_equal(out.cpu().numpy(), sup_ref)
+    finally:
+        L.tdt_set_support_caps(0, 0)
+
+
+def test_deterministic_at_scale():
+    """R-MAT scale 17 (rows above the warp threshold): two runs agree, and
+    agree with the oracle."""
+    s, d = G.rmat_edges(17, 16 << 17, seed=1)
+    pairs = np.stack([s, d], 1)
+    rows, cols, rp, verts = O.preprocess(pairs)
+    assert np.diff(rp).max() > 256
+    g = graph_of(rows, cols, rp)
+    a = T.truss_decompose(g, lists=True)
+    b = T.truss_decompose(g, lists=True)
+    c = T.truss_decompose(g, lists=False)
+    assert torch.equal(a.truss, b.truss) and torch.equal(a.e_truss, b.e_truss)
+    assert torch.equal(a.truss, c.truss) and torch.equal(a.e_truss, c.e_truss)
+    _oracle_check(pairs)
+
+
+def _books(copies, k, pages, seed=0):
+    """copies of K_k with `pages` extra vertices glued to every clique edge:
+    each glued edge lies in one triangle, so level 1 queues long runs of
+    edges owning a single triangle-list slot each."""
+    rng = np.random.default_rng(seed)
+    edges, base = [], 0
+    for _ in range(copies):
+        nxt = base + k
+        for a in range(k):
+            for b in range(a + 1, k):
+                edges.append((base + a, base + b))
+                for _ in range(pages):
+                    edges += [(base + a, nxt), (base + b, nxt)]
+                    nxt += 1
+        base = nxt
+    perm = rng.permutation(base)
+    return perm[np.array(edges, dtype=np.int64)].astype(np.int32)
+
+
+def test_listed_peel_long_runs_of_unit_items():
+    """336K frontier edges with one list slot each: every warp walks several
+    windows of single-slot items (regression test of the window advance)."""
+    pairs = _books(2000, 8, 3)
+    _oracle_check(pairs)
+    rows, cols, rp, verts = O.preprocess(pairs)
+    g = graph_of(rows, cols, rp)
+    a = T.truss_decompose(g, lists=True)
+    b = T.truss_decompose(g, lists=True)
     assert torch.equal(a.truss, b.truss) and torch.equal(a.e_truss, b.e_truss)
