@@ -230,6 +230,23 @@ int tdt_triangle_count(const int32_t *cols, const int64_t *row_ptr, int64_t num_
                        int64_t num_edges, int32_t *support, int64_t *stats, void *workspace,
                        size_t workspace_bytes, tdt_stream_t stream);
 
+/* Triangle count that allocates no device memory.  It has no counterpart in
+ * the reference; it is for callers that cannot call cudaMalloc where they
+ * need the count (another component owns the device allocator, or the path
+ * must not stall on an allocation).  Same outputs as tdt_triangle_count
+ * (support may be NULL; stats[TDT_STAT_TRIANGLES], stats[TDT_STAT_STATUS]),
+ * but the scratch is a fixed 24 MiB array inside the library, held on every
+ * GPU that loads it until the process exits.  Limit: at most 2^18 vertices
+ * and 2^18 edges; larger graphs return TDT_ERR_INVALID (use
+ * tdt_triangle_count).  The first call on a device looks up that array's
+ * address (cudaGetSymbolAddress) with the device current; make that first
+ * call before any stream capture.  All calls share the array and each call
+ * re-initialises what it uses, so two calls that overlap on the same GPU
+ * (for example on two streams) race on it and must be serialised by the
+ * caller. */
+int tdt_triangle_count_noalloc(const int32_t *cols, const int64_t *row_ptr, int64_t num_vertices,
+                               int64_t num_edges, int32_t *support, int64_t *stats, tdt_stream_t stream);
+
 /* k-truss search (ktruss_search/ktruss_cuda.py:383-463 with l = k-2):
  * in_ktruss[i] = 1 when edge i belongs to the k-truss, else 0;
  * stats[TDT_STAT_ALIVE] = its edge count. */

@@ -54,6 +54,7 @@ _SIGS = [
     ("tdt_truss_decompose", ctypes.c_int,
      [c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_size, c_ptr]),
     ("tdt_triangle_count", ctypes.c_int, [c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr, c_size, c_ptr]),
+    ("tdt_triangle_count_noalloc", ctypes.c_int, [c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr]),
     ("tdt_ktruss_search", ctypes.c_int,
      [c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_i32, c_ptr, c_ptr, c_ptr, c_size, c_ptr]),
 ]
