@@ -186,6 +186,25 @@ int tdt_sub_affected_support_tile(const int32_t *sub_rows, const int32_t *sub_co
  * Whole-path entry points (the device-resident hot path).
  * ===================================================================== */
 
+/* Preprocessing: raw edge list -> degree-oriented CSRCOO on the device.
+ * Restates read_prepro_save (singlegpu_truss.py:172-178): Graph.read_edgelist
+ * (src/type/Graph_Truss.py:177-213: drop self-loops, dedup unordered pairs,
+ * rank vertices by degree) + CSRCOO.edge_list_to_Graph / counter_sort
+ * (src/type/CSRCOO.py:128-177: relabel by rank, orient low->high, CSR sorted
+ * by (row, column)).  Degree ties go to the smaller id (the reference's numpy
+ * argsort is unstable); with vertex_group (int32[num_ids], may be NULL) the
+ * rank key is (group, degree, id), so a batch of graphs keeps contiguous
+ * ranges.  Inputs: src/dst int32[num_draws] with ids in [0, num_ids).
+ * Outputs: rows/cols int32[num_draws] (first E_out used), row_ptr
+ * int64[num_ids+1] (first V_out+1 used), vertices int32[num_ids] (original id
+ * of each rank), counts int64[3] = {E_out, V_out, status} (device).  No host
+ * synchronisation inside. */
+size_t tdt_preprocess_workspace_bytes(int64_t num_draws, int64_t num_ids);
+int tdt_preprocess(const int32_t *src, const int32_t *dst, int64_t num_draws, int64_t num_ids,
+                   const int32_t *vertex_group, int32_t num_groups, int32_t *rows, int32_t *cols,
+                   int64_t *row_ptr, int32_t *vertices, int64_t *counts, void *workspace,
+                   size_t workspace_bytes, tdt_stream_t stream);
+
 /* Layout of the int64 `stats` words the whole-path calls write (device). */
 enum tdt_stat_index {
     TDT_STAT_STATUS = 0,     /* 0 = ok, else a tdt_status raised on the device */

@@ -50,6 +50,9 @@ _SIGS = [
     ("tdt_sub_affected_support", ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr]),
     ("tdt_sub_affected_support_tile", ctypes.c_int,
      [c_ptr, c_ptr, c_ptr, c_i64, c_i32, c_ptr, c_ptr, c_i64, c_ptr]),
+    ("tdt_preprocess_workspace_bytes", c_size, [c_i64, c_i64]),
+    ("tdt_preprocess", ctypes.c_int,
+     [c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_size, c_ptr]),
     ("tdt_decompose_workspace_bytes", c_size, [c_i64, c_i64]),
     ("tdt_truss_decompose", ctypes.c_int,
      [c_ptr, c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_size, c_ptr]),

@@ -1,0 +1,88 @@
+"""Batched truss decomposition of many graphs in one device-resident run.
+
+A batch of oriented graphs whose vertex ranges (and so edge ranges) are
+disjoint and increasing is itself one oriented CSR: the disjoint union.  Truss
+numbers are properties of each connected component, and every sub-round of
+the union peels, in each graph, exactly the edges that graph's own run would
+peel in its sub-round of the same level.  So one tdt_truss_decompose call over
+the union decomposes every graph of the batch: one support launch, one
+listing launch and ONE persistent cooperative peel launch for thousands of
+graphs of uneven size (the plain path runs those launches, plus a host sync,
+per graph).  Per-graph results are slices of the union's: truss[eb[g]:eb[g+1]]
+and kmax[g] = max of that slice.
+"""
+from typing import List, NamedTuple
+
+import numpy as np
+import torch
+
+from . import truss as T
+from .graph import CSRCOO
+
+
+class GraphBatch(NamedTuple):
+    graph: CSRCOO              # the disjoint union (int64 row_ptr)
+    vertex_offsets: torch.Tensor  # int64[G+1] (host)
+    edge_offsets: torch.Tensor    # int64[G+1] (host)
+
+    @property
+    def num_graphs(self):
+        return self.edge_offsets.numel() - 1
+
+
+class BatchResult(NamedTuple):
+    truss: torch.Tensor        # int32[E_total], graph g owns [edge_offsets[g], edge_offsets[g+1])
+    kmax: torch.Tensor         # int64[G] (device)
+    union: T.TrussResult
+
+
+def pack_host(graphs, device="cuda", pin=True):
+    """graphs: list of (rows, cols, row_ptr) numpy arrays of oriented graphs
+    (local vertex ids).  Packs them on the host into one union (vertex ids of
+    graph g shifted by its vertex offset) and copies it to the device in three
+    transfers."""
+    G = len(graphs)
+    vo = np.zeros(G + 1, np.int64)
+    eo = np.zeros(G + 1, np.int64)
+    for g, (r, c, rp) in enumerate(graphs):
+        vo[g + 1] = vo[g] + (len(rp) - 1)
+        eo[g + 1] = eo[g] + len(c)
+    rows = np.empty(eo[-1], np.int32)
+    cols = np.empty(eo[-1], np.int32)
+    rpu = np.empty(vo[-1] + 1, np.int64)
+    for g, (r, c, rp) in enumerate(graphs):
+        rows[eo[g]:eo[g + 1]] = np.asarray(r) + vo[g]
+        cols[eo[g]:eo[g + 1]] = np.asarray(c) + vo[g]
+        rpu[vo[g]:vo[g + 1]] = np.asarray(rp[:-1], np.int64) + eo[g]
+    rpu[-1] = eo[-1]
+    ts = [torch.from_numpy(x) for x in (rows, cols, rpu)]
+    if pin:
+        ts = [t.pin_memory() for t in ts]
+    rows_d, cols_d, rp_d = (t.to(device, non_blocking=True) for t in ts)
+    return GraphBatch(CSRCOO(columns=cols_d, row_ptr=rp_d, rows=rows_d), torch.from_numpy(vo),
+                      torch.from_numpy(eo))
+
+
+def batch_from_union(graph, edge_offsets, vertex_offsets):
+    """Wrap an already packed union (e.g. preprocessed on the device with
+    vertex groups) as a GraphBatch."""
+    return GraphBatch(graph, torch.as_tensor(vertex_offsets, dtype=torch.int64).cpu(),
+                      torch.as_tensor(edge_offsets, dtype=torch.int64).cpu())
+
+
+def decompose(batch, workspace=None, lists="auto", sync=True):
+    """Decompose every graph of the batch in one device-resident run."""
+    res = T.truss_decompose(batch.graph, workspace=workspace, lists=lists, sync=sync)
+    tr = res.truss if sync else res[0]
+    eo = batch.edge_offsets.to(tr.device)
+    G = batch.num_graphs
+    seg = torch.repeat_interleave(torch.arange(G, device=tr.device), eo[1:] - eo[:-1])
+    kmax = torch.full((G,), 2, dtype=torch.int64, device=tr.device)
+    kmax.scatter_reduce_(0, seg, tr.to(torch.int64), reduce="amax", include_self=True)
+    return BatchResult(tr, kmax, res)
+
+
+def per_graph(batch: GraphBatch, result: BatchResult, g: int):
+    """Truss numbers of graph g (its own CSR edge order)."""
+    a, b = int(batch.edge_offsets[g]), int(batch.edge_offsets[g + 1])
+    return result.truss[a:b]
