@@ -70,9 +70,9 @@ def batch_from_union(graph, edge_offsets, vertex_offsets):
                       torch.as_tensor(edge_offsets, dtype=torch.int64).cpu())
 
 
-def decompose(batch, workspace=None, lists="auto", sync=True):
+def decompose(batch, workspace=None, lists="auto", sync=True, list_budget=None):
     """Decompose every graph of the batch in one device-resident run."""
-    res = T.truss_decompose(batch.graph, workspace=workspace, lists=lists, sync=sync)
+    res = T.truss_decompose(batch.graph, workspace=workspace, lists=lists, sync=sync, list_budget=list_budget)
     tr = res.truss if sync else res[0]
     eo = batch.edge_offsets.to(tr.device)
     G = batch.num_graphs

@@ -105,12 +105,15 @@ def _check_stats(stats_host, where):
         raise _lib.TdtError(st, where, "reported by the device")
 
 
-def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto"):
+def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto", list_budget=None):
     """Full truss decomposition (singlegpu_truss.py:67-158 + :38-45).
 
     lists: "auto" keeps per-edge triangle lists in the workspace when they fit
     in LIST_BUDGET_FRACTION of the free device memory (the first call on a
-    graph then counts its triangles first), True always, False never."""
+    graph then counts its triangles first), True always, False never.
+    list_budget (bytes): instead, give the lists a fixed workspace tail and
+    let the device decide (lists when 24 T bytes fit, else the search peel),
+    with no counting pass."""
     L = _lib.load()
     rows, cols, rp = _graph_arrays(graph)
     dev = cols.device
@@ -123,7 +126,8 @@ def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto")
     need = L.tdt_decompose_workspace_bytes(V, E)
     wso = _ws_for(dev, workspace)
     base = (need + 255) // 256 * 256
-    ws = wso.get(base + _list_bytes(wso, cols, rp, lists, base))
+    tail = int(list_budget) if list_budget is not None else _list_bytes(wso, cols, rp, lists, base)
+    ws = wso.get(base + tail)
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
     rc = L.tdt_truss_decompose(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
                                truss.data_ptr(), e_truss.data_ptr(), ptr.data_ptr(), cap, stats.data_ptr(),
