@@ -49,6 +49,7 @@ struct PeelCtl {
     unsigned long long q[3];      // packed (items << kCandBits | candidates) per round slot
     unsigned long long fe[3];     // frontier edges per round slot (queued or not)
     int min_sup[2];
+    unsigned long long n_alive[2];  // lengths of the two alive-edge lists
     int listed;                   // 1: per-edge triangle lists were built (they fit the workspace)
     int list_skip;                // gate of the listing pass and of the list-only setup kernels
     int enum_skip;                // gate of the in-adjacency build (needed without lists)
@@ -56,6 +57,9 @@ struct PeelCtl {
     long long rounds;
     long long triangles;
     unsigned long long alive;
+    // block 0's time (ns) in candidate processing, grid-barrier waits after
+    // processing, and level transitions; diagnostic only
+    unsigned long long t_proc, t_wait, t_trans, t_total;
 };
 
 struct PeelArgs {
@@ -70,6 +74,8 @@ struct PeelArgs {
     int32_t* round_level;
     int4* qi[2];
     long long* qb[2];
+    int32_t* alive[2];    // compacted alive-edge lists (level transitions)
+    int* blk_cnt;         // survivors per block in a transition
     const int64_t* off;   // listed mode: list offsets int64[E+1]
     const int2* lists;    // listed mode: partner edge pairs
     int64_t V, E, round_cap;
@@ -145,46 +151,111 @@ __device__ __forceinline__ bool dec_support(const PeelArgs& A, int64_t x, int32_
     return false;
 }
 
+// Block-wide exclusive scan of one int per thread; returns the prefix and
+// writes the block total to *total.
+__device__ __forceinline__ int block_excl_scan_int(int v, int* s_w, int* total) {
+    const unsigned lane = lane_id();
+    const int w = threadIdx.x / kWarp;
+    int incl = warp_incl_scan(v);
+    if (lane == 31) s_w[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int x = lane < kPeelWarps ? s_w[lane] : 0;
+        int xi = warp_incl_scan(x);
+        if (lane < kPeelWarps) s_w[lane] = xi - x;
+        if (lane == kPeelWarps - 1) s_w[kPeelWarps] = xi;
+    }
+    __syncthreads();
+    const int r = s_w[w] + incl - v;
+    *total = s_w[kPeelWarps];
+    __syncthreads();
+    return r;
+}
+
 // Level transition (decomposition mode): l = min support over alive edges,
 // F_{r_next} = alive edges with support l.  Returns false when no edge is alive.
+// The alive edges are kept in a compacted list in ascending edge order:
+// transition t reads list t&1 (all edge ids at t = 0), each block owning one
+// contiguous chunk.  Pass 1 finds the minimum support and the number of
+// survivors per block; after the barrier every block knows its output offset,
+// and pass 2 writes its survivors, in order, to list (t+1)&1 and collects the
+// frontier.  Both passes stream sequentially through the edges still alive.
 __device__ bool level_transition(const PeelArgs& A, int r_next, int ntrans, int32_t* l_out) {
     __shared__ int s_min[kPeelWarps];
+    __shared__ int s_w[kPeelWarps + 1];
+    __shared__ long long s_off;
     const unsigned lane = lane_id();
     const int wib = threadIdx.x / kWarp;
     const int p = ntrans & 1;
+    const bool first = ntrans == 0;
+    const int32_t* cur = A.alive[p];
+    int32_t* nxt = A.alive[p ^ 1];
+    const long long ncur = first ? A.E : (long long)__ldcg(&A.ctl->n_alive[p]);
+    const long long chunk = (ncur + gridDim.x - 1) / gridDim.x;
+    const long long c0 = (long long)blockIdx.x * chunk;
+    const long long c1 = c0 + chunk < ncur ? c0 + chunk : ncur;
     if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl->min_sup[p ^ 1] = INT32_MAX;
-    int mn = INT32_MAX;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < A.E;
-         e += (int64_t)gridDim.x * blockDim.x) {
+    // pass 1: minimum support and survivor count of this block's chunk
+    int mn = INT32_MAX, cnt = 0;
+    for (long long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+        const int32_t e = first ? (int32_t)i : __ldcg(cur + i);
         if (__ldcg(A.rnd + e) == -1) {
+            cnt++;
             const int32_t s = __ldcg(A.sup + e);
             mn = s < mn ? s : mn;
         }
     }
     mn = warp_min(mn);
-    if (lane == 0) s_min[wib] = mn;
+    cnt = warp_sum(cnt);
+    if (lane == 0) { s_min[wib] = mn; s_w[wib] = cnt; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        int b = INT32_MAX;
-        for (int i = 0; i < kPeelWarps; i++) b = s_min[i] < b ? s_min[i] : b;
+        int b = INT32_MAX, c = 0;
+        for (int i = 0; i < kPeelWarps; i++) { b = s_min[i] < b ? s_min[i] : b; c += s_w[i]; }
         if (b != INT32_MAX) atomicMin(&A.ctl->min_sup[p], b);
+        A.blk_cnt[blockIdx.x] = c;
     }
     if (!grid_barrier(&A.ctl->g, gridDim.x)) return false;
     const int l = *(volatile int*)&A.ctl->min_sup[p];
     if (l == INT32_MAX) return false;
     *l_out = l;
-    const int slot = r_next % 3, buf = r_next & 1;
-    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; base < A.E;
-         base += nthreads) {
-        const int64_t e = base + lane;
-        bool want = false;
-        int32_t s = 0;
-        if (e < A.E && __ldcg(A.rnd + e) == -1) {
-            s = __ldcg(A.sup + e);
-            if (s <= l) { want = true; A.rnd[e] = r_next; }
+    // output offset of this block = survivors of the blocks before it
+    {
+        long long part = 0;
+        for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) part += __ldcg(A.blk_cnt + b);
+        part = warp_sum(part);
+        if (lane == 0) s_min[wib] = (int)part;  // per-warp partials fit int (< E)
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            long long o = 0;
+            for (int i = 0; i < kPeelWarps; i++) o += s_min[i];
+            s_off = o;
+            if (blockIdx.x == gridDim.x - 1) A.ctl->n_alive[p ^ 1] = (unsigned long long)(o + A.blk_cnt[blockIdx.x]);
+            if (blockIdx.x == 0) A.ctl->n_alive[p] = 0;
         }
-        warp_append(A, slot, buf, want, (int32_t)e, s);
+        __syncthreads();
+    }
+    long long out = s_off;
+    // pass 2: ordered survivors + the frontier (support <= l)
+    const int slot = r_next % 3, buf = r_next & 1;
+    for (long long base = c0; base < c1; base += blockDim.x) {
+        const long long i = base + threadIdx.x;
+        int32_t e = 0, s = 0;
+        bool keep = false;
+        if (i < c1) {
+            e = first ? (int32_t)i : __ldcg(cur + i);
+            if (__ldcg(A.rnd + e) == -1) {
+                keep = true;
+                s = __ldcg(A.sup + e);
+            }
+        }
+        int tot;
+        const int pos = block_excl_scan_int(keep ? 1 : 0, s_w, &tot);
+        if (keep) nxt[out + pos] = e;
+        out += tot;
+        const bool want = keep && s <= l;
+        if (want) A.rnd[e] = r_next;
+        warp_append(A, slot, buf, want, e, s);
     }
     return grid_barrier(&A.ctl->g, gridDim.x);
 }
@@ -232,6 +303,7 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
         if (master) A.ctl->rounds = 0;
         return;
     }
+    uint64_t t_mark = globaltimer_ns();
     for (;;) {
         if (master) {
             A.round_level[r] = l;
@@ -317,20 +389,24 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
                         const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
                         if (af && ag) {
                             const bool ff = rf == r, fg = rg == r;
-                            if (!ff && !fg) {
-                                want_f = dec_support(A, f, l, r + 1);
-                                want_g = dec_support(A, g, l, r + 1);
-                            } else if (ff && !fg) {
-                                if (e < f) want_g = dec_support(A, g, l, r + 1);
-                            } else if (!ff && fg) {
-                                if (e < g) want_f = dec_support(A, f, l, r + 1);
-                            }
+                            // which of f, g this lane decrements (ownership rules above)
+                            const bool df = !ff && (!fg || e < g);
+                            const bool dg = !fg && (!ff || e < f);
+                            // issue both atomics before using either result
+                            int32_t of = 0, og = 0;
+                            if (df) of = atomicSub(A.sup + f, 1);
+                            if (dg) og = atomicSub(A.sup + g, 1);
+                            want_f = df && of == l + 1;
+                            want_g = dg && og == l + 1;
+                            if (want_f) A.rnd[f] = r + 1;
+                            if (want_g) A.rnd[g] = r + 1;
                         }
                     }
                 }
             }
             warp_append(A, nslot, nbuf, want_f, (int32_t)f, l);
             warp_append(A, nslot, nbuf, want_g, (int32_t)g, l);
+
             {
                 // the next window starts at the item of slot cb+32 (<= i0+32)
                 int jn = 0;
@@ -348,7 +424,14 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
             }
             __syncwarp();
         }
+        __syncthreads();
+        const uint64_t t_p = globaltimer_ns();
         if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
+        const uint64_t t_b = globaltimer_ns();
+        if (master) {
+            A.ctl->t_proc += t_p - t_mark;
+            A.ctl->t_wait += t_b - t_p;
+        }
         if (r + 2 >= A.round_cap) {
             if (master) set_status(A.ctl, TDT_ERR_CAPACITY);
             return;
@@ -357,12 +440,18 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
         if (nfe == 0) {
             if (A.mode != 0) break;
             int32_t nl;
-            if (!level_transition(A, r + 1, ntrans++, &nl)) break;
+            const bool more = level_transition(A, r + 1, ntrans++, &nl);
+            if (master) A.ctl->t_trans += globaltimer_ns() - t_b;
+            if (!more) break;
             l = nl;
         }
+        t_mark = globaltimer_ns();
         r++;
     }
-    if (master) A.ctl->rounds = r + 1;
+    if (master) {
+        A.ctl->rounds = r + 1;
+        A.ctl->t_total = globaltimer_ns() - t_start;
+    }
 }
 
 // ------------------------------------------------------------------ setup / output kernels
@@ -614,6 +703,8 @@ struct Layout {
     int4* qi[2];
     long long* qb[2];
     int64_t* off;
+    int32_t* alive[2];
+    int* blk_cnt;
     void* scan_ws;
     void* sort_ws;
     size_t total;
@@ -638,6 +729,9 @@ Layout carve(void* ws, int64_t V, int64_t E) {
         L.qb[b] = (long long*)c.take(8 * e);
     }
     L.off = (int64_t*)c.take(8 * (e + 1));
+    L.alive[0] = (int32_t*)c.take(4 * e);
+    L.alive[1] = (int32_t*)c.take(4 * e);
+    L.blk_cnt = (int*)c.take(4 * 4096);
     size_t scan_b = scan_scratch_bytes((int64_t)(e > v ? e : v) + 1);
     L.scan_ws = c.take(scan_b);
     L.sort_ws = c.take(radix_sort_scratch_bytes((int64_t)e));
@@ -750,10 +844,13 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     A.sup = L.sup; A.rnd = L.rnd; A.round_level = L.round_level;
     A.qi[0] = L.qi[0]; A.qi[1] = L.qi[1]; A.qb[0] = L.qb[0]; A.qb[1] = L.qb[1];
     A.off = L.off; A.lists = lists;
+    A.alive[0] = L.alive[0]; A.alive[1] = L.alive[1];
+    A.blk_cnt = L.blk_cnt;
     A.V = V; A.E = E; A.round_cap = E + 2;
     A.mode = mode == 0 ? 0 : 1;
     A.fixed_level = fixed_level;
     A.ctl = L.ctl;
+    if (di.sms * occ > 4096) occ = 4096 / di.sms;
     dim3 grid(di.sms * occ), block(kPeelBlock);
     void* args[] = {&A};
     TDT_CUDA(cudaLaunchCooperativeKernel((void*)peel_kernel, grid, block, args, 0, st));

@@ -34,9 +34,10 @@ namespace tdt {
 
 constexpr int kSupBlock = 512;                 // 16 warps
 constexpr int kSupWarps = kSupBlock / kWarp;
-constexpr int kWarpCap = 256;                  // light rows: d+(u) <= kWarpCap
 constexpr int kVertexBatch = 8;                // vertices per dynamic grab
-constexpr int kSupSmemBytes = 96 * 1024;       // dynamic shared memory per block
+// 48 KB of dynamic shared memory per block: with ~6 KB static, four blocks
+// (64 warps, full occupancy at <= 32 registers) fit the SM's 228 KB
+constexpr int kSupSmemBytes = 48 * 1024;
 constexpr int kHeavyChunk = 16;                // vertices scanned per phase-1 grab
 
 enum SupMode { kSupAccum = 0, kSupRoles = 1, kSupList = 2 };
@@ -51,6 +52,13 @@ template <int M>
 struct HeavyCap {
     static constexpr int value = (kSupSmemBytes - 1024) / (RowBytes<M>::value + 12);
 };
+// light rows (d+(u) <= WarpCap) get one warp and a per-warp shared slice
+template <int M>
+struct WarpCap {
+    static constexpr int value = M == kSupList ? 128 : 256;
+};
+static_assert(RowBytes<kSupList>::value * WarpCap<kSupList>::value * kSupWarps <= kSupSmemBytes, "list slices");
+static_assert(RowBytes<kSupRoles>::value * WarpCap<kSupRoles>::value * kSupWarps <= kSupSmemBytes, "role slices");
 
 // Row ranges are clamped to [0, ne] so a malformed row_ptr cannot move an
 // access outside cols/out.
@@ -375,7 +383,7 @@ __global__ void __launch_bounds__(kSupBlock) support_kernel(OutRows<Off> G, SupA
 
     // ---- phase 2: rows with 2 <= d+(u) <= kWarpCap, one warp per row, taken
     // in batches from the top ids (highest degree rank) down
-    unsigned char* wbuf = smem + wib * (RowBytes<M>::value * kWarpCap);
+    unsigned char* wbuf = smem + wib * (RowBytes<M>::value * WarpCap<M>::value);
     const long long gw = (long long)blockIdx.x * kSupWarps + wib;
     const long long nw = (long long)gridDim.x * kSupWarps;
     for (long long it = 0;; it++) {
@@ -393,7 +401,7 @@ __global__ void __launch_bounds__(kSupBlock) support_kernel(OutRows<Off> G, SupA
             const Off bu = G.begin(uu);
             const int d = (int)(G.end(uu) - bu);
             if (d < 2 || d > warp_cap) continue;
-            RowState<M> R = stage_row<M>(G, A, wbuf, kWarpCap, true, bu, d, lane, kWarp);
+            RowState<M> R = stage_row<M>(G, A, wbuf, WarpCap<M>::value, true, bu, d, lane, kWarp);
             __syncwarp();
             wedge_walk<M, kIdOrdered>(G, A, R, d, 0, kWarp, s_excl[wib], s_bv[wib]);
             __syncwarp();
@@ -409,10 +417,11 @@ static int launch_mode(const OutRows<Off>& G, const SupArgs& A, SupCtl* ctl, cud
     int rc = device_info(&di);
     if (rc) return rc;
     SupArgs A2 = A;
-    A2.warp_cap = (g_warp_cap > 0 && g_warp_cap < kWarpCap) ? g_warp_cap : kWarpCap;
+    A2.warp_cap = (g_warp_cap > 0 && g_warp_cap < WarpCap<M>::value) ? g_warp_cap : WarpCap<M>::value;
     A2.heavy_cap = (g_heavy_cap > 0 && g_heavy_cap < HeavyCap<M>::value) ? g_heavy_cap : HeavyCap<M>::value;
     auto kern = support_kernel<M, kIdOrdered, Off>;
     TDT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSupSmemBytes));
+    TDT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     if (ctl) TDT_CUDA(cudaMemsetAsync(ctl, 0, sizeof(SupCtl), st));
     int blocks_per_sm = 0;
     TDT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kSupBlock, kSupSmemBytes));
