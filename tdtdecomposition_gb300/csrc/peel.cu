@@ -48,8 +48,12 @@ struct PeelCtl {
     GridCtl g;
     unsigned long long q[3];      // packed (items << kCandBits | candidates) per round slot
     unsigned long long fe[3];     // frontier edges per round slot (queued or not)
-    int min_sup[2];
-    unsigned long long n_alive[2];  // lengths of the two alive-edge lists
+    unsigned long long cnt[3];     // survivors written by level change t, at t % 3
+    unsigned long long side_n[3];  // side-list length of level-change pass k, at k % 3
+    unsigned long long pfe[3];     // edges queued by level-change pass k, at k % 3
+    int mgt[3];                    // minimum support found by level-change pass k, at k % 3
+    int dmin[2];                   // minimum decrement result above the level during level L_t, at t & 1
+    long long passes;              // level-change passes run (diagnostic)
     int listed;                   // 1: per-edge triangle lists were built (they fit the workspace)
     int list_skip;                // gate of the listing pass and of the list-only setup kernels
     int enum_skip;                // gate of the in-adjacency build (needed without lists)
@@ -69,13 +73,11 @@ struct PeelArgs {
     const int64_t* cp;
     const int32_t* in_src;
     const int32_t* in_eid;
-    int32_t* sup;
-    int32_t* rnd;
+    int2* es;             // edge state {support, round}: round -1 = alive, else the sub-round that peeled it
     int32_t* round_level;
     int4* qi[2];
     long long* qb[2];
     int32_t* alive[2];    // compacted alive-edge lists (level transitions)
-    int* blk_cnt;         // survivors per block in a transition
     const int64_t* off;   // listed mode: list offsets int64[E+1]
     const int2* lists;    // listed mode: partner edge pairs
     int64_t V, E, round_cap;
@@ -93,14 +95,15 @@ __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long
     return __ldcg(p);
 }
 
-// Queue the edges flagged by `want` (one per lane) for the round in `slot`.
-// cur_sup is the edge's support at marking time (0 => no alive triangle).
+// Queue the edges flagged by `want` (one per lane) for the round in `slot`
+// and add their number to *nfront.  cur_sup is the edge's support at marking
+// time (0 => no alive triangle).
 __device__ __forceinline__ void warp_append(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
-                                            int32_t cur_sup) {
+                                            int32_t cur_sup, unsigned long long* nfront) {
     const unsigned lane = lane_id();
     const unsigned mf = __ballot_sync(kFull, want);
     if (mf == 0) return;
-    if (lane == (unsigned)(__ffs(mf) - 1)) atomicAdd(&A.ctl->fe[slot], (unsigned long long)__popc(mf));
+    if (lane == (unsigned)(__ffs(mf) - 1)) atomicAdd(nfront, (unsigned long long)__popc(mf));
     int32_t x = 0, y = 0, dxo = 0;
     long long dx = 0;
     bool q = want && cur_sup > 0;
@@ -141,122 +144,178 @@ __device__ __forceinline__ void warp_append(const PeelArgs& A, int slot, int buf
     }
 }
 
-// One decrement; returns true when the edge crossed from l+1 to l.
-__device__ __forceinline__ bool dec_support(const PeelArgs& A, int64_t x, int32_t l, int r_next) {
-    const int32_t old = atomicSub(A.sup + x, 1);
-    if (old == l + 1) {
-        A.rnd[x] = r_next;
-        return true;
-    }
-    return false;
+// Level changes (decomposition mode).  Level change t starts level L_t =
+// min support over the alive edges and queues F = alive edges with support
+// L_t.  The alive edges live in a compacted list (list t&1 is the input of
+// change t, all edge ids at t = 0).
+//
+// One streaming pass usually suffices: a lower bound g of L_t is known before
+// the pass (0 at t = 0; afterwards the minimum support above L_{t-1} seen at
+// change t-1, lowered by every decrement result above L_{t-1} during level
+// L_{t-1}).  The pass compacts the survivors into list (t+1)&1, queues the
+// alive edges with support == g, collects those with support in (g, g+W) in
+// a side list, and takes the minimum support above g.  If anything was
+// queued, L_t = g.  Otherwise L_t = that minimum, and its frontier is found
+// in the side list (or, past the window, by one more pass over the compacted
+// list).  Every pass k ends with a grid barrier and writes its minimum,
+// side-list length and queued count to slot k % 3 of mgt / side_n / pfe; the
+// block-0 thread that clears slot (k+1) % 3 at the start of pass k clears a
+// slot that every block finished reading before the barrier of pass k-1.
+constexpr int kSideWindow = 64;
+
+// Fold a per-lane minimum into *dst: one atomic per warp, skipped when *dst
+// is already no larger (a plain read keeps ten thousand warps from
+// serialising on one address).
+__device__ __forceinline__ void fold_min(int* dst, int32_t v) {
+    v = warp_min(v);
+    if (lane_id() == 0 && v != INT32_MAX && v < *(volatile int*)dst) atomicMin(dst, v);
 }
 
-// Block-wide exclusive scan of one int per thread; returns the prefix and
-// writes the block total to *total.
-__device__ __forceinline__ int block_excl_scan_int(int v, int* s_w, int* total) {
-    const unsigned lane = lane_id();
-    const int w = threadIdx.x / kWarp;
-    int incl = warp_incl_scan(v);
-    if (lane == 31) s_w[w] = incl;
-    __syncthreads();
-    if (w == 0) {
-        int x = lane < kPeelWarps ? s_w[lane] : 0;
-        int xi = warp_incl_scan(x);
-        if (lane < kPeelWarps) s_w[lane] = xi - x;
-        if (lane == kPeelWarps - 1) s_w[kPeelWarps] = xi;
+__device__ __forceinline__ void pass_min(const PeelArgs& A, int np, int32_t v) { fold_min(&A.ctl->mgt[np % 3], v); }
+
+// Level-change passes stream the alive list in steps of kStep x 32 entries per
+// warp: the gathers of a step are in flight together and the step reserves its
+// output ranges with one atomic each.
+#ifndef TDT_PEEL_STEP
+#define TDT_PEEL_STEP 8
+#endif
+constexpr int kStep = TDT_PEEL_STEP;
+
+__device__ __forceinline__ void pass_start(const PeelArgs& A, int np) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        A.ctl->mgt[(np + 1) % 3] = INT32_MAX;
+        A.ctl->side_n[(np + 1) % 3] = 0;
+        A.ctl->pfe[(np + 1) % 3] = 0;
+        A.ctl->passes++;
     }
-    __syncthreads();
-    const int r = s_w[w] + incl - v;
-    *total = s_w[kPeelWarps];
-    __syncthreads();
-    return r;
 }
 
-// Level transition (decomposition mode): l = min support over alive edges,
-// F_{r_next} = alive edges with support l.  Returns false when no edge is alive.
-// The alive edges are kept in a compacted list in ascending edge order:
-// transition t reads list t&1 (all edge ids at t = 0), each block owning one
-// contiguous chunk.  Pass 1 finds the minimum support and the number of
-// survivors per block; after the barrier every block knows its output offset,
-// and pass 2 writes its survivors, in order, to list (t+1)&1 and collects the
-// frontier.  Both passes stream sequentially through the edges still alive.
-__device__ bool level_transition(const PeelArgs& A, int r_next, int ntrans, int32_t* l_out) {
-    __shared__ int s_min[kPeelWarps];
-    __shared__ int s_w[kPeelWarps + 1];
-    __shared__ long long s_off;
+__device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int t, int& np, int32_t* l_out) {
     const unsigned lane = lane_id();
-    const int wib = threadIdx.x / kWarp;
-    const int p = ntrans & 1;
-    const bool first = ntrans == 0;
+    const long long gw = (long long)blockIdx.x * kPeelWarps + threadIdx.x / kWarp;
+    const long long nw = (long long)gridDim.x * kPeelWarps;
+    const int p = t & 1;
+    const bool first = t == 0;
     const int32_t* cur = A.alive[p];
     int32_t* nxt = A.alive[p ^ 1];
-    const long long ncur = first ? A.E : (long long)__ldcg(&A.ctl->n_alive[p]);
-    const long long chunk = (ncur + gridDim.x - 1) / gridDim.x;
-    const long long c0 = (long long)blockIdx.x * chunk;
-    const long long c1 = c0 + chunk < ncur ? c0 + chunk : ncur;
-    if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl->min_sup[p ^ 1] = INT32_MAX;
-    // pass 1: minimum support and survivor count of this block's chunk
-    int mn = INT32_MAX, cnt = 0;
-    for (long long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
-        const int32_t e = first ? (int32_t)i : __ldcg(cur + i);
-        if (__ldcg(A.rnd + e) == -1) {
-            cnt++;
-            const int32_t s = __ldcg(A.sup + e);
-            mn = s < mn ? s : mn;
-        }
+    const long long ncur = first ? A.E : (long long)__ldcg(&A.ctl->cnt[(t + 2) % 3]);
+    int32_t g = 0;
+    if (!first) {
+        const int32_t a = *(volatile int*)&A.ctl->mgt[(np + 2) % 3];
+        const int32_t b = *(volatile int*)&A.ctl->dmin[(t + 1) & 1];
+        g = a < b ? a : b;
     }
-    mn = warp_min(mn);
-    cnt = warp_sum(cnt);
-    if (lane == 0) { s_min[wib] = mn; s_w[wib] = cnt; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int b = INT32_MAX, c = 0;
-        for (int i = 0; i < kPeelWarps; i++) { b = s_min[i] < b ? s_min[i] : b; c += s_w[i]; }
-        if (b != INT32_MAX) atomicMin(&A.ctl->min_sup[p], b);
-        A.blk_cnt[blockIdx.x] = c;
-    }
-    if (!grid_barrier(&A.ctl->g, gridDim.x)) return false;
-    const int l = *(volatile int*)&A.ctl->min_sup[p];
-    if (l == INT32_MAX) return false;
-    *l_out = l;
-    // output offset of this block = survivors of the blocks before it
-    {
-        long long part = 0;
-        for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) part += __ldcg(A.blk_cnt + b);
-        part = warp_sum(part);
-        if (lane == 0) s_min[wib] = (int)part;  // per-warp partials fit int (< E)
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            long long o = 0;
-            for (int i = 0; i < kPeelWarps; i++) o += s_min[i];
-            s_off = o;
-            if (blockIdx.x == gridDim.x - 1) A.ctl->n_alive[p ^ 1] = (unsigned long long)(o + A.blk_cnt[blockIdx.x]);
-            if (blockIdx.x == 0) A.ctl->n_alive[p] = 0;
-        }
-        __syncthreads();
-    }
-    long long out = s_off;
-    // pass 2: ordered survivors + the frontier (support <= l)
+    const int32_t gw_end = g > INT32_MAX - kSideWindow ? INT32_MAX : g + kSideWindow;
     const int slot = r_next % 3, buf = r_next & 1;
-    for (long long base = c0; base < c1; base += blockDim.x) {
-        const long long i = base + threadIdx.x;
-        int32_t e = 0, s = 0;
-        bool keep = false;
-        if (i < c1) {
-            e = first ? (int32_t)i : __ldcg(cur + i);
-            if (__ldcg(A.rnd + e) == -1) {
-                keep = true;
-                s = __ldcg(A.sup + e);
+    int2* side = reinterpret_cast<int2*>(A.qi[buf ^ 1]);  // the finished round's queue is free
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        A.ctl->cnt[(t + 1) % 3] = 0;
+        A.ctl->dmin[t & 1] = INT32_MAX;
+    }
+    pass_start(A, np);
+    // pass 1: compact, queue support == g, side-list the window, minimum above g
+    {
+        int32_t mloc = INT32_MAX;
+        unsigned long long* ocnt = &A.ctl->cnt[t % 3];
+        unsigned long long* scnt = &A.ctl->side_n[np % 3];
+        const unsigned lt = lanemask_lt();
+        for (long long base = gw * (kWarp * kStep); base < ncur; base += nw * (kWarp * kStep)) {
+            int32_t e[kStep], sv[kStep];
+            bool keep[kStep];
+#pragma unroll
+            for (int u = 0; u < kStep; u++) {
+                const long long i = base + u * kWarp + lane;
+                e[u] = 0;
+                if (i < ncur) e[u] = first ? (int32_t)i : __ldcg(cur + i);
+            }
+#pragma unroll
+            for (int u = 0; u < kStep; u++) {
+                const long long i = base + u * kWarp + lane;
+                keep[u] = false;
+                sv[u] = 0;
+                if (i < ncur) {
+                    const int2 st = __ldcg(A.es + e[u]);
+                    keep[u] = st.y == -1;
+                    sv[u] = st.x;
+                }
+            }
+            unsigned km[kStep], wm[kStep];
+            int nk = 0, nwin = 0;
+#pragma unroll
+            for (int u = 0; u < kStep; u++) {
+                km[u] = __ballot_sync(kFull, keep[u]);
+                wm[u] = __ballot_sync(kFull, keep[u] && sv[u] > g && sv[u] < gw_end);
+                nk += __popc(km[u]);
+                nwin += __popc(wm[u]);
+                if (keep[u] && sv[u] > g) mloc = sv[u] < mloc ? sv[u] : mloc;
+            }
+            unsigned long long ok = 0, os = 0;
+            if (lane == 0) {
+                if (nk) ok = atomicAdd(ocnt, (unsigned long long)nk);
+                if (nwin) os = atomicAdd(scnt, (unsigned long long)nwin);
+            }
+            ok = __shfl_sync(kFull, ok, 0);
+            os = __shfl_sync(kFull, os, 0);
+#pragma unroll
+            for (int u = 0; u < kStep; u++) {
+                if (keep[u]) nxt[ok + __popc(km[u] & lt)] = e[u];
+                if ((wm[u] >> lane) & 1u) side[os + __popc(wm[u] & lt)] = make_int2(e[u], sv[u]);
+                ok += __popc(km[u]);
+                os += __popc(wm[u]);
+                const bool want = keep[u] && sv[u] == g;
+                if (want) A.es[e[u]].y = r_next;
+                warp_append(A, slot, buf, want, e[u], sv[u], &A.ctl->pfe[np % 3]);
             }
         }
-        int tot;
-        const int pos = block_excl_scan_int(keep ? 1 : 0, s_w, &tot);
-        if (keep) nxt[out + pos] = e;
-        out += tot;
-        const bool want = keep && s <= l;
-        if (want) A.rnd[e] = r_next;
-        warp_append(A, slot, buf, want, e, s);
+        pass_min(A, np, mloc);
     }
+    np++;
+    if (!grid_barrier(&A.ctl->g, gridDim.x)) return false;
+    if (ld_cg_u64(&A.ctl->pfe[(np + 2) % 3]) > 0) {
+        *l_out = g;
+        return true;
+    }
+    const int32_t m = *(volatile int*)&A.ctl->mgt[(np + 2) % 3];
+    if (m == INT32_MAX) return false;  // no edge is alive
+    *l_out = m;
+    pass_start(A, np);
+    int32_t mloc = INT32_MAX;
+    if (m < gw_end) {
+        // pass 2a: the frontier is in the side list; edges outside it have
+        // support >= g + W, which bounds the next minimum from below
+        const long long ns = (long long)__ldcg(&A.ctl->side_n[(np + 2) % 3]);
+        mloc = gw_end;
+        for (long long base = gw * kWarp; base < ns; base += nw * kWarp) {
+            const long long i = base + lane;
+            int32_t e = 0, sv = INT32_MAX;
+            if (i < ns) {
+                const int2 x = __ldcg(side + i);
+                e = x.x;
+                sv = x.y;
+            }
+            const bool want = i < ns && sv == m;
+            if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
+            if (want) A.es[e].y = r_next;
+            warp_append(A, slot, buf, want, e, sv, &A.ctl->pfe[np % 3]);
+        }
+    } else {
+        // pass 2b: one more pass over the compacted list
+        const long long n2 = (long long)__ldcg(&A.ctl->cnt[t % 3]);
+        for (long long base = gw * kWarp; base < n2; base += nw * kWarp) {
+            const long long i = base + lane;
+            int32_t e = 0, sv = INT32_MAX;
+            if (i < n2) {
+                e = __ldcg(nxt + i);
+                sv = __ldcg(&A.es[e].x);
+            }
+            const bool want = i < n2 && sv == m;
+            if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
+            if (want) A.es[e].y = r_next;
+            warp_append(A, slot, buf, want, e, sv, &A.ctl->pfe[np % 3]);
+        }
+    }
+    pass_min(A, np, mloc);
+    np++;
     return grid_barrier(&A.ctl->g, gridDim.x);
 }
 
@@ -270,18 +329,145 @@ __device__ bool fixed_start(const PeelArgs& A, int32_t l) {
         bool want = false;
         int32_t s = 0;
         if (e < A.E) {
-            s = __ldcg(A.sup + e);
-            if (s <= l) { want = true; A.rnd[e] = 0; }
+            s = __ldcg(&A.es[e].x);
+            if (s <= l) { want = true; A.es[e].y = 0; }
         }
-        warp_append(A, 0, 0, want, (int32_t)e, s);
+        warp_append(A, 0, 0, want, (int32_t)e, s, &A.ctl->fe[0]);
     }
     return grid_barrier(&A.ctl->g, gridDim.x);
 }
 
-__global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
+// One sub-round: warps gwarp = 0..nwarps-1 share the candidate slots of round r.
+// The smallest decrement result above l is folded into *dmin (the lower bound
+// of the next level).
+__device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp,
+                                              long long nwarps, long long* s_win, int* dmin) {
+    const unsigned lane = lane_id();
+    int32_t dm = INT32_MAX;
+    const int slot = r % 3, buf = r & 1;
+    const int nslot = (r + 1) % 3, nbuf = buf ^ 1;
+    const unsigned long long packed = ld_cg_u64(&A.ctl->q[slot]);
+    const long long N = (long long)(packed >> kCandBits);
+    const long long T = (long long)(packed & kCandMask);
+    const long long* __restrict__ qb = A.qb[buf];
+    const int4* __restrict__ qi = A.qi[buf];
+    // each warp owns a contiguous range of candidate slots; the owning item
+    // of its first slot is found once, later ones by sliding the window
+    const long long per_warp = (((T + nwarps - 1) / nwarps) + 31) & ~31ll;
+    const long long cb0 = gwarp * per_warp;
+    const long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
+    long long i0 = 0;
+    if (cb0 < cb1) {
+        if (lane == 0) {
+            long long lo = 0, hi = N - 1;
+            while (lo < hi) {
+                long long mid = (lo + hi + 1) >> 1;
+                if (__ldcg(qb + mid) <= cb0) lo = mid; else hi = mid - 1;
+            }
+            i0 = lo;
+        }
+        i0 = __shfl_sync(kFull, i0, 0);
+    }
+    for (long long cb = cb0; cb < cb1; cb += kWarp) {
+        s_win[lane] = (i0 + lane < N) ? __ldcg(qb + i0 + lane) : LLONG_MAX;
+        __syncwarp();
+        const long long t = cb + lane;
+        bool want_f = false, want_g = false;
+        int64_t f = 0, g = 0;
+        // window index of this lane's item: slot cb lies in item i0 and each
+        // item owns >= 1 slot, so slot cb+k lies in item i0+k at most; the
+        // window holds i0..i0+31, and i0+32 is checked with one more load
+        int jl = 0;
+        long long base_l = 0;
+        {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (s_win[mid] <= t) lo = mid; else hi = mid - 1;
+            }
+            jl = lo;
+            base_l = s_win[lo];
+            if (lo == 31 && i0 + 32 < N) {
+                const long long nb = __ldcg(qb + i0 + 32);
+                if (nb <= t) { jl = 32; base_l = nb; }
+            }
+        }
+        if (t < cb1) {
+            const int lo = jl;
+            const long long item = i0 + lo;
+            const int4 it = __ldcg(qi + item);
+            const int32_t e = it.x, x = it.y, y = it.z, dxo = it.w;
+            const long long tl = t - base_l;
+            int32_t w = y;
+            if (A.lists) {
+                // listed mode: the slot is one of e's triangles, (f, g) its other edges
+                const int2 fg = __ldg(A.lists + __ldg(A.off + e) + tl);
+                f = fg.x;
+                g = fg.y;
+                w = ~y;  // any value != y
+            } else if (tl < dxo) {
+                f = __ldg(A.rp + x) + tl;
+                w = __ldg(A.cols + f);
+            } else {
+                const int64_t k = __ldg(A.cp + x) + (tl - dxo);
+                w = __ldg(A.in_src + k);
+                f = __ldg(A.in_eid + k);
+            }
+            if (w != y) {
+                if (!A.lists)
+                    g = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
+                                : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
+                if (g >= 0) {
+                    const int32_t rf = __ldcg(&A.es[f].y), rg = __ldcg(&A.es[g].y);
+                    const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
+                    if (af && ag) {
+                        const bool ff = rf == r, fg = rg == r;
+                        // which of f, g this lane decrements (ownership rules above)
+                        const bool df = !ff && (!fg || e < g);
+                        const bool dg = !fg && (!ff || e < f);
+                        // issue both atomics before using either result
+                        int32_t of = 0, og = 0;
+                        if (df) of = atomicSub(&A.es[f].x, 1);
+                        if (dg) og = atomicSub(&A.es[g].x, 1);
+                        want_f = df && of == l + 1;
+                        want_g = dg && og == l + 1;
+                        if (df && of > l + 1) dm = of - 1 < dm ? of - 1 : dm;
+                        if (dg && og > l + 1) dm = og - 1 < dm ? og - 1 : dm;
+                        if (want_f) A.es[f].y = r + 1;
+                        if (want_g) A.es[g].y = r + 1;
+                    }
+                }
+            }
+        }
+        warp_append(A, nslot, nbuf, want_f, (int32_t)f, l, &A.ctl->fe[nslot]);
+        warp_append(A, nslot, nbuf, want_g, (int32_t)g, l, &A.ctl->fe[nslot]);
+
+        {
+            // the next window starts at the item of slot cb+32 (<= i0+32)
+            int jn = 0;
+            if (lane == 31) {
+                const long long tn = cb + kWarp;
+                int lo = 0, hi = 31;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (s_win[mid] <= tn) lo = mid; else hi = mid - 1;
+                }
+                jn = lo;
+                if (lo == 31 && i0 + 32 < N && __ldcg(qb + i0 + 32) <= tn) jn = 32;
+            }
+            i0 += __shfl_sync(kFull, jn, 31);
+        }
+        __syncwarp();
+    }
+    fold_min(dmin, dm);
+}
+
+#ifndef TDT_PEEL_MINB
+#define TDT_PEEL_MINB 2
+#endif
+__global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArgs A) {
     __shared__ long long s_win[kPeelWarps][kWarp];
     if (!*(volatile int*)&A.ctl->listed) A.lists = nullptr;
-    const unsigned lane = lane_id();
     const int wib = threadIdx.x / kWarp;
     const int64_t gwarp = (int64_t)blockIdx.x * kPeelWarps + wib;
     const int64_t nwarps = (int64_t)gridDim.x * kPeelWarps;
@@ -291,10 +477,10 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
     const uint64_t t_start = globaltimer_ns();
     int r = 0;
     int32_t l = 0;
-    int ntrans = 0;
+    int ntrans = 0, np = 0;
     bool ok;
     if (A.mode == 0) {
-        ok = level_transition(A, 0, ntrans++, &l);
+        ok = level_transition(A, 0, ntrans++, np, &l);
     } else {
         l = A.fixed_level;
         ok = fixed_start(A, l);
@@ -311,119 +497,8 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
             A.ctl->fe[(r + 2) % 3] = 0;
             if (globaltimer_ns() - t_start > kPeelDeadlineNs) set_status(A.ctl, TDT_ERR_TIMEOUT);
         }
-        const int slot = r % 3, buf = r & 1;
-        const int nslot = (r + 1) % 3, nbuf = buf ^ 1;
-        const unsigned long long packed = ld_cg_u64(&A.ctl->q[slot]);
-        const long long N = (long long)(packed >> kCandBits);
-        const long long T = (long long)(packed & kCandMask);
-        const long long* __restrict__ qb = A.qb[buf];
-        const int4* __restrict__ qi = A.qi[buf];
-        // each warp owns a contiguous range of candidate slots; the owning item
-        // of its first slot is found once, later ones by sliding the window
-        const long long per_warp = (((T + nwarps - 1) / nwarps) + 31) & ~31ll;
-        const long long cb0 = gwarp * per_warp;
-        const long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
-        long long i0 = 0;
-        if (cb0 < cb1) {
-            if (lane == 0) {
-                long long lo = 0, hi = N - 1;
-                while (lo < hi) {
-                    long long mid = (lo + hi + 1) >> 1;
-                    if (__ldcg(qb + mid) <= cb0) lo = mid; else hi = mid - 1;
-                }
-                i0 = lo;
-            }
-            i0 = __shfl_sync(kFull, i0, 0);
-        }
-        for (long long cb = cb0; cb < cb1; cb += kWarp) {
-            s_win[wib][lane] = (i0 + lane < N) ? __ldcg(qb + i0 + lane) : LLONG_MAX;
-            __syncwarp();
-            const long long t = cb + lane;
-            bool want_f = false, want_g = false;
-            int64_t f = 0, g = 0;
-            // window index of this lane's item: slot cb lies in item i0 and each
-            // item owns >= 1 slot, so slot cb+k lies in item i0+k at most; the
-            // window holds i0..i0+31, and i0+32 is checked with one more load
-            int jl = 0;
-            long long base_l = 0;
-            {
-                int lo = 0, hi = 31;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (s_win[wib][mid] <= t) lo = mid; else hi = mid - 1;
-                }
-                jl = lo;
-                base_l = s_win[wib][lo];
-                if (lo == 31 && i0 + 32 < N) {
-                    const long long nb = __ldcg(qb + i0 + 32);
-                    if (nb <= t) { jl = 32; base_l = nb; }
-                }
-            }
-            if (t < cb1) {
-                const int lo = jl;
-                const long long item = i0 + lo;
-                const int4 it = __ldcg(qi + item);
-                const int32_t e = it.x, x = it.y, y = it.z, dxo = it.w;
-                const long long tl = t - base_l;
-                int32_t w = y;
-                if (A.lists) {
-                    // listed mode: the slot is one of e's triangles, (f, g) its other edges
-                    const int2 fg = __ldg(A.lists + __ldg(A.off + e) + tl);
-                    f = fg.x;
-                    g = fg.y;
-                    w = ~y;  // any value != y
-                } else if (tl < dxo) {
-                    f = __ldg(A.rp + x) + tl;
-                    w = __ldg(A.cols + f);
-                } else {
-                    const int64_t k = __ldg(A.cp + x) + (tl - dxo);
-                    w = __ldg(A.in_src + k);
-                    f = __ldg(A.in_eid + k);
-                }
-                if (w != y) {
-                    if (!A.lists)
-                        g = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
-                                    : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
-                    if (g >= 0) {
-                        const int32_t rf = __ldcg(A.rnd + f), rg = __ldcg(A.rnd + g);
-                        const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
-                        if (af && ag) {
-                            const bool ff = rf == r, fg = rg == r;
-                            // which of f, g this lane decrements (ownership rules above)
-                            const bool df = !ff && (!fg || e < g);
-                            const bool dg = !fg && (!ff || e < f);
-                            // issue both atomics before using either result
-                            int32_t of = 0, og = 0;
-                            if (df) of = atomicSub(A.sup + f, 1);
-                            if (dg) og = atomicSub(A.sup + g, 1);
-                            want_f = df && of == l + 1;
-                            want_g = dg && og == l + 1;
-                            if (want_f) A.rnd[f] = r + 1;
-                            if (want_g) A.rnd[g] = r + 1;
-                        }
-                    }
-                }
-            }
-            warp_append(A, nslot, nbuf, want_f, (int32_t)f, l);
-            warp_append(A, nslot, nbuf, want_g, (int32_t)g, l);
-
-            {
-                // the next window starts at the item of slot cb+32 (<= i0+32)
-                int jn = 0;
-                if (lane == 31) {
-                    const long long tn = cb + kWarp;
-                    int lo = 0, hi = 31;
-                    while (lo < hi) {
-                        int mid = (lo + hi + 1) >> 1;
-                        if (s_win[wib][mid] <= tn) lo = mid; else hi = mid - 1;
-                    }
-                    jn = lo;
-                    if (lo == 31 && i0 + 32 < N && __ldcg(qb + i0 + 32) <= tn) jn = 32;
-                }
-                i0 += __shfl_sync(kFull, jn, 31);
-            }
-            __syncwarp();
-        }
+        // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
+        process_round(A, r, l, gwarp, nwarps, s_win[wib], &A.ctl->dmin[(ntrans + 1) & 1]);
         __syncthreads();
         const uint64_t t_p = globaltimer_ns();
         if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
@@ -436,11 +511,12 @@ __global__ void __launch_bounds__(kPeelBlock) peel_kernel(PeelArgs A) {
             if (master) set_status(A.ctl, TDT_ERR_CAPACITY);
             return;
         }
-        const unsigned long long nfe = ld_cg_u64(&A.ctl->fe[nslot]);
-        if (nfe == 0) {
+        // fe[(r+1) % 3] is only written by sub-round r (level changes count
+        // into pfe), and cleared again at the top of sub-round r+2
+        if (ld_cg_u64(&A.ctl->fe[(r + 1) % 3]) == 0) {
             if (A.mode != 0) break;
             int32_t nl;
-            const bool more = level_transition(A, r + 1, ntrans++, &nl);
+            const bool more = level_transition(A, r + 1, ntrans++, np, &nl);
             if (master) A.ctl->t_trans += globaltimer_ns() - t_b;
             if (!more) break;
             l = nl;
@@ -510,22 +586,23 @@ __global__ void csc_fill_kernel(const int32_t* __restrict__ rows, const int32_t*
     }
 }
 
-// sup = cA + cB + cC (the role counts of the support pass), rnd = alive,
-// triangle total.
+// sup = cA + cB + cC (the role counts of the support pass), edge state =
+// {sup, alive}, triangle total.
 __global__ void init_state_kernel(const int32_t* __restrict__ cA, const int32_t* __restrict__ cB,
                                   const int32_t* __restrict__ cC, int32_t* __restrict__ sup,
-                                  int32_t* __restrict__ rnd, int64_t E, PeelCtl* ctl) {
+                                  int2* __restrict__ es, int64_t E, PeelCtl* ctl) {
     __shared__ long long s_part[32];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        ctl->min_sup[0] = INT32_MAX;
-        ctl->min_sup[1] = INT32_MAX;
+        for (int i = 0; i < 3; i++) ctl->mgt[i] = INT32_MAX;
+        ctl->dmin[0] = INT32_MAX;
+        ctl->dmin[1] = INT32_MAX;
     }
     long long acc = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t s = cA[e] + cB[e] + cC[e];
         sup[e] = s;
-        rnd[e] = -1;
+        es[e] = make_int2(s, -1);
         acc += s;
     }
     acc = warp_sum(acc);
@@ -580,13 +657,13 @@ __global__ void list_check_kernel(const int64_t* __restrict__ off, const int32_t
     }
 }
 
-__global__ void truss_out_kernel(const int32_t* __restrict__ rnd, const int32_t* __restrict__ round_level,
+__global__ void truss_out_kernel(const int2* __restrict__ es, const int32_t* __restrict__ round_level,
                                  int64_t E, int32_t* __restrict__ truss, uint32_t* __restrict__ keys,
                                  uint32_t* __restrict__ vals, PeelCtl* ctl) {
     if (ctl->g.status != 0) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t r = rnd[e];
+        const int32_t r = es[e].y;
         if (r < 0) {  // every edge is peeled when the run completes
             atomicMax((int*)&ctl->g.status, (int)TDT_ERR_CAPACITY);
             continue;
@@ -638,13 +715,13 @@ __global__ void ptr_etruss_kernel(const uint32_t* __restrict__ keys, const uint3
     }
 }
 
-__global__ void ktruss_out_kernel(const int32_t* __restrict__ rnd, int64_t E, uint8_t* __restrict__ in_k,
+__global__ void ktruss_out_kernel(const int2* __restrict__ es, int64_t E, uint8_t* __restrict__ in_k,
                                   PeelCtl* ctl) {
     __shared__ unsigned long long s_part[32];
     unsigned long long acc = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const uint8_t a = rnd[e] == -1;
+        const uint8_t a = es[e].y == -1;
         in_k[e] = a;
         acc += a;
     }
@@ -669,6 +746,7 @@ __global__ void stats_final_kernel(PeelCtl* ctl, int64_t* stats, int mode) {
 
 // ------------------------------------------------------------------ host side
 void prof_mark(int phase, cudaStream_t st);
+
 int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* cA, int32_t* cB,
                          int32_t* cC, void* ctl, const int* gate, cudaStream_t st);
 int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* off,
@@ -698,13 +776,12 @@ struct Layout {
     int32_t* in_src;
     int32_t* in_eid;
     int32_t* sup;
-    int32_t* rnd;
+    int2* es;
     int32_t* round_level;
     int4* qi[2];
     long long* qb[2];
     int64_t* off;
     int32_t* alive[2];
-    int* blk_cnt;
     void* scan_ws;
     void* sort_ws;
     size_t total;
@@ -722,7 +799,7 @@ Layout carve(void* ws, int64_t V, int64_t E) {
     L.in_src = (int32_t*)c.take(4 * e);
     L.in_eid = (int32_t*)c.take(4 * e);
     L.sup = (int32_t*)c.take(4 * e);
-    L.rnd = (int32_t*)c.take(4 * e);
+    L.es = (int2*)c.take(8 * e);
     L.round_level = (int32_t*)c.take(4 * (e + 2));
     for (int b = 0; b < 2; b++) {
         L.qi[b] = (int4*)c.take(16 * e);
@@ -731,7 +808,6 @@ Layout carve(void* ws, int64_t V, int64_t E) {
     L.off = (int64_t*)c.take(8 * (e + 1));
     L.alive[0] = (int32_t*)c.take(4 * e);
     L.alive[1] = (int32_t*)c.take(4 * e);
-    L.blk_cnt = (int*)c.take(4 * 4096);
     size_t scan_b = scan_scratch_bytes((int64_t)(e > v ? e : v) + 1);
     L.scan_ws = c.take(scan_b);
     L.sort_ws = c.take(radix_sort_scratch_bytes((int64_t)e));
@@ -793,7 +869,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     prof_mark(0, st);
     rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->g.status, st);
     if (rc) return rc;
-    init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.rnd, E, L.ctl);
+    init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
     TDT_LAUNCH_CHECK("init_state");
     prof_mark(1, st);
     if (mode == 2) {
@@ -841,11 +917,10 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     }
     PeelArgs A;
     A.rp = rp; A.cols = cols; A.rows = rows_use; A.cp = L.cp; A.in_src = L.in_src; A.in_eid = L.in_eid;
-    A.sup = L.sup; A.rnd = L.rnd; A.round_level = L.round_level;
+    A.es = L.es; A.round_level = L.round_level;
     A.qi[0] = L.qi[0]; A.qi[1] = L.qi[1]; A.qb[0] = L.qb[0]; A.qb[1] = L.qb[1];
     A.off = L.off; A.lists = lists;
     A.alive[0] = L.alive[0]; A.alive[1] = L.alive[1];
-    A.blk_cnt = L.blk_cnt;
     A.V = V; A.E = E; A.round_cap = E + 2;
     A.mode = mode == 0 ? 0 : 1;
     A.fixed_level = fixed_level;
@@ -863,7 +938,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
         uint32_t* vals = keys + E;
         uint32_t* keys_alt = reinterpret_cast<uint32_t*>(L.qi[1]);
         uint32_t* vals_alt = keys_alt + E;
-        truss_out_kernel<<<g_e, tb, 0, st>>>(L.rnd, L.round_level, E, truss, keys, vals, L.ctl);
+        truss_out_kernel<<<g_e, tb, 0, st>>>(L.es, L.round_level, E, truss, keys, vals, L.ctl);
         TDT_LAUNCH_CHECK("truss_out");
         const uint32_t* sk = keys;
         const uint32_t* sv = vals;
@@ -879,7 +954,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
         stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 0);
         TDT_LAUNCH_CHECK("stats_final");
     } else {
-        ktruss_out_kernel<<<g_e, tb, 0, st>>>(L.rnd, E, in_k, L.ctl);
+        ktruss_out_kernel<<<g_e, tb, 0, st>>>(L.es, E, in_k, L.ctl);
         TDT_LAUNCH_CHECK("ktruss_out");
         stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 1);
         TDT_LAUNCH_CHECK("stats_final");

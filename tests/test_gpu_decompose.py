@@ -229,3 +229,20 @@ def test_listed_peel_long_runs_of_unit_items():
     a = T.truss_decompose(g, lists=True)
     b = T.truss_decompose(g, lists=True)
     assert torch.equal(a.truss, b.truss) and torch.equal(a.e_truss, b.e_truss)
+
+
+def test_level_gaps_vs_oracle():
+    """Disjoint cliques K_4, K_9, K_40, K_120, K_230 plus a sparse random
+    part: consecutive levels, gaps inside the level-change side window
+    (64) and gaps beyond it."""
+    rng = np.random.default_rng(11)
+    edges, base = [], 0
+    for k in (4, 9, 40, 120, 230):
+        a, b = np.triu_indices(k, 1)
+        edges.append(np.stack([a + base, b + base], 1))
+        base += k
+    n = 3000
+    edges.append(rng.integers(base, base + n, size=(12000, 2)))
+    pairs = np.concatenate(edges).astype(np.int32)
+    pairs = rng.permutation(base + n).astype(np.int32)[pairs]
+    _oracle_check(pairs)
