@@ -108,7 +108,11 @@ __device__ __forceinline__ void warp_append(const PeelArgs& A, int slot, int buf
     long long dx = 0;
     bool q = want && cur_sup > 0;
     if (q && A.lists) {
-        dx = __ldg(A.off + e + 1) - __ldg(A.off + e);  // the edge's original triangles
+        // the edge's original triangles; the item carries the list offset
+        const long long o = __ldg(A.off + e);
+        dx = __ldg(A.off + e + 1) - o;
+        x = (int32_t)(unsigned)(o & 0xffffffffll);
+        y = (int32_t)(o >> 32);
         if (dx <= 0) q = false;
     } else if (q) {
         const int32_t u = __ldg(A.rows + e), v = __ldg(A.cols + e);
@@ -213,13 +217,20 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
         A.ctl->dmin[t & 1] = INT32_MAX;
     }
     pass_start(A, np);
-    // pass 1: compact, queue support == g, side-list the window, minimum above g
+    // pass 1: compact, queue support == g, side-list the window, minimum above g.
+    // Blocks take tiles of kPeelWarps x kStep x 32 entries; each tile reserves
+    // its survivor and side-list ranges with one atomic each.
     {
+        __shared__ int s_tk[kPeelWarps], s_tw[kPeelWarps];
+        __shared__ unsigned long long s_base[2];
+        constexpr long long kTile = (long long)kPeelWarps * kStep * kWarp;
+        const int wib = threadIdx.x / kWarp;
         int32_t mloc = INT32_MAX;
         unsigned long long* ocnt = &A.ctl->cnt[t % 3];
         unsigned long long* scnt = &A.ctl->side_n[np % 3];
         const unsigned lt = lanemask_lt();
-        for (long long base = gw * (kWarp * kStep); base < ncur; base += nw * (kWarp * kStep)) {
+        for (long long tb = (long long)blockIdx.x * kTile; tb < ncur; tb += (long long)gridDim.x * kTile) {
+            const long long base = tb + (long long)wib * (kStep * kWarp);
             int32_t e[kStep], sv[kStep];
             bool keep[kStep];
 #pragma unroll
@@ -249,13 +260,26 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
                 nwin += __popc(wm[u]);
                 if (keep[u] && sv[u] > g) mloc = sv[u] < mloc ? sv[u] : mloc;
             }
-            unsigned long long ok = 0, os = 0;
             if (lane == 0) {
-                if (nk) ok = atomicAdd(ocnt, (unsigned long long)nk);
-                if (nwin) os = atomicAdd(scnt, (unsigned long long)nwin);
+                s_tk[wib] = nk;
+                s_tw[wib] = nwin;
             }
-            ok = __shfl_sync(kFull, ok, 0);
-            os = __shfl_sync(kFull, os, 0);
+            __syncthreads();
+            if (wib == 0) {
+                const int a = lane < kPeelWarps ? s_tk[lane] : 0, b = lane < kPeelWarps ? s_tw[lane] : 0;
+                const int ai = warp_incl_scan(a), bi = warp_incl_scan(b);
+                if (lane == kPeelWarps - 1) {
+                    s_base[0] = ai ? atomicAdd(ocnt, (unsigned long long)ai) : 0ull;
+                    s_base[1] = bi ? atomicAdd(scnt, (unsigned long long)bi) : 0ull;
+                }
+                if (lane < kPeelWarps) {
+                    s_tk[lane] = ai - a;
+                    s_tw[lane] = bi - b;
+                }
+            }
+            __syncthreads();
+            unsigned long long ok = s_base[0] + (unsigned long long)s_tk[wib];
+            unsigned long long os = s_base[1] + (unsigned long long)s_tw[wib];
 #pragma unroll
             for (int u = 0; u < kStep; u++) {
                 if (keep[u]) nxt[ok + __popc(km[u] & lt)] = e[u];
@@ -266,6 +290,7 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
                 if (want) A.es[e[u]].y = r_next;
                 warp_append(A, slot, buf, want, e[u], sv[u], &A.ctl->pfe[np % 3]);
             }
+            __syncthreads();  // s_tk / s_base are reused by the next tile
         }
         pass_min(A, np, mloc);
     }
@@ -401,7 +426,8 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
             int32_t w = y;
             if (A.lists) {
                 // listed mode: the slot is one of e's triangles, (f, g) its other edges
-                const int2 fg = __ldg(A.lists + __ldg(A.off + e) + tl);
+                const long long lo = (long long)(unsigned)x | ((long long)y << 32);
+                const int2 fg = __ldg(A.lists + lo + tl);
                 f = fg.x;
                 g = fg.y;
                 w = ~y;  // any value != y
