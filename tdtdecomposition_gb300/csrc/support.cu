@@ -7,13 +7,18 @@
 //
 // Here the unit of work is the source vertex u of the triangle (u, v, w)
 // (u -> v, u -> w, v -> w):
-//   * N+(u) is staged once in shared memory (warp slice for d+(u) <= kWarpCap,
-//     the whole block's buffer for larger rows; rows beyond the block buffer
-//     are searched in place);
-//   * the warp walks the flattened list of all (v, w) with v in N+(u) and
-//     w in N+(v), 32 consecutive entries per step (coalesced loads of N+(v)),
-//     and looks each w up in N+(u) by binary search (restricted to the
-//     entries after v when the orientation is by vertex id);
+//   * N+(u) is staged once in shared memory (one warp for d+(u) <= warp_cap,
+//     a whole block for larger rows; rows beyond the block buffer are searched
+//     in place), with a bitmap of its hashed vertex ids;
+//   * the wedges (v, w), v in N+(u), w in N+(v), form one flat index space
+//     (the out-lists of a group of v's back to back: 32 v's for a warp, 512 for
+//     a block).  A warp walks it 32 consecutive wedges per step (coalesced
+//     loads of N+(v)); the owner v of each lane's wedge comes from one
+//     OR-reduction of the group boundaries inside the step, not a search;
+//   * w is tested against the bitmap; most wedges close no triangle and stop
+//     there.  Candidates go to a per-warp queue in shared memory and are
+//     resolved 32 at a time by binary search in N+(u) (full warps instead of a
+//     few active lanes);
 //   * hits on (u,v) and (u,w) go to shared-memory counters flushed once per
 //     row; only the (v,w) hit is a global atomic.
 // Each triangle is found exactly once, from its (source, middle) edge, so the
@@ -26,7 +31,7 @@
 //   kSupList   per-edge triangle lists: the entry of edge e in triangle
 //              (eA, eB, eC) holds the two other edges; e's list occupies
 //              [off[e], off[e+1]) with its role-A entries first, then role B,
-//              then role C.  Slots of roles A and B come from per-row cursors
+//              then role C.  Slots of roles A and B come from per-row counters
 //              in shared memory, role C from a global cursor.
 #include "common.cuh"
 
@@ -34,31 +39,44 @@ namespace tdt {
 
 constexpr int kSupBlock = 512;                 // 16 warps
 constexpr int kSupWarps = kSupBlock / kWarp;
-constexpr int kVertexBatch = 8;                // vertices per dynamic grab
-// 48 KB of dynamic shared memory per block: with ~6 KB static, four blocks
-// (64 warps, full occupancy at <= 32 registers) fit the SM's 228 KB
-constexpr int kSupSmemBytes = 48 * 1024;
-constexpr int kHeavyChunk = 16;                // vertices scanned per phase-1 grab
+constexpr int kSupMinBlocks = 3;               // resident blocks per SM (registers <= 42)
+constexpr int kSupSmemBytes = 64 * 1024;       // dynamic shared memory per block
+constexpr int kVertexBatch = 8;                // light vertices per dynamic grab
+constexpr int kHeavyChunk = 16;                // vertices scanned per heavy grab
+constexpr int kQueue = 64;                     // candidate queue entries per warp
+
+// Light rows: one warp, a 4 KB slice of the block buffer:
+//   su[256] | cnt[256] | group S[32] VI[32] BV[32] | bitmap 8192 bits | queue
+constexpr int kWarpCap = 256;
+constexpr int kSliceBytes = kSupSmemBytes / kSupWarps;
+constexpr int kLightBmLog2 = 13;
+constexpr int kSlSu = 0;
+constexpr int kSlCnt = kSlSu + 4 * kWarpCap;
+constexpr int kSlS = kSlCnt + 4 * kWarpCap;
+constexpr int kSlVI = kSlS + 4 * kWarp;
+constexpr int kSlBV = kSlVI + 4 * kWarp;
+constexpr int kSlBm = kSlBV + 8 * kWarp;
+constexpr int kSlQ = kSlBm + (1 << kLightBmLog2) / 8;
+static_assert(kSlQ + 8 * kQueue <= kSliceBytes, "light slice");
+
+// Heavy rows: one block, the whole buffer:
+//   su[H] | cnt[H] | group S[512] VI[512] BV[512] | bitmap 2^16 bits | queues
+// Rows longer than H are searched in place (su and counters in global memory)
+// with a 2^18-bit bitmap over the su/cnt area.
+constexpr int kSeg = kSupBlock;                // v's per heavy group (one per thread)
+constexpr int kHeavyBmLog2 = 16;
+constexpr int kHugeBmLog2 = 18;
+constexpr int kHvQueues = kSupSmemBytes - kSupWarps * 8 * kQueue;
+constexpr int kHvBm = kHvQueues - (1 << kHeavyBmLog2) / 8;
+constexpr int kHvBV = kHvBm - 8 * kSeg;
+constexpr int kHvVI = kHvBV - 4 * kSeg;
+constexpr int kHvS = kHvVI - 4 * kSeg;
+constexpr int kHeavyCap = kHvS / 8;            // su + cnt, 8 bytes per entry
+static_assert(kHeavyCap >= 4096, "heavy cap");
+static_assert((1 << kHugeBmLog2) / 8 <= kHvS, "in-place bitmap");
+static_assert(kHeavyCap < 65536, "packed 16-bit role counters");
 
 enum SupMode { kSupAccum = 0, kSupRoles = 1, kSupList = 2 };
-
-// shared-memory bytes per staged row entry (light rows: row + counters; heavy
-// rows add the pair-space prefix (4 B) and the out-list start of each v (8 B))
-template <int M>
-struct RowBytes {
-    static constexpr int value = M == kSupAccum ? 8 : (M == kSupRoles ? 12 : 20);
-};
-template <int M>
-struct HeavyCap {
-    static constexpr int value = (kSupSmemBytes - 1024) / (RowBytes<M>::value + 12);
-};
-// light rows (d+(u) <= WarpCap) get one warp and a per-warp shared slice
-template <int M>
-struct WarpCap {
-    static constexpr int value = M == kSupList ? 128 : 256;
-};
-static_assert(RowBytes<kSupList>::value * WarpCap<kSupList>::value * kSupWarps <= kSupSmemBytes, "list slices");
-static_assert(RowBytes<kSupRoles>::value * WarpCap<kSupRoles>::value * kSupWarps <= kSupSmemBytes, "role slices");
 
 // Row ranges are clamped to [0, ne] so a malformed row_ptr cannot move an
 // access outside cols/out.
@@ -85,14 +103,14 @@ struct SupArgs {
     const int64_t* off;             // kSupList: list offsets int64[E+1]
     const int32_t* cA_in;           // kSupList: role-A counts (role-B base = off + cA)
     const int32_t* cB_in;           // kSupList: role-B counts (end-of-row check)
-    unsigned long long* curA_g;     // kSupList: global cursors for rows beyond the smem cap
+    unsigned long long* curA_g;     // kSupList: global cursors for rows searched in place
     unsigned long long* curB_g;
     unsigned long long* curC;       // kSupList: role-C cursors, start at off + cA + cB
     int2* lists;
     const int* gate;                // non-zero: skip the pass
     int* status;                    // kSupList: set when a row's slots do not end where counted
     int warp_cap;                   // rows with d+ <= warp_cap go to one warp (<= kWarpCap)
-    int heavy_cap;                  // heavier rows staged in smem up to this size (<= the mode's cap)
+    int heavy_cap;                  // heavier rows staged in smem up to this size (<= kHeavyCap)
 };
 
 // Test hook: lower the light/heavy thresholds so small graphs drive every path
@@ -108,6 +126,10 @@ struct SupCtl {
     unsigned long long light_next;
 };
 
+__device__ __forceinline__ uint32_t bm_hash(int32_t w, int log2bits) {
+    return ((uint32_t)w * 0x9E3779B1u) >> (32 - log2bits);
+}
+
 // Binary search of key in s[lo, hi) (shared or global, generic address).
 __device__ __forceinline__ int bsearch_i32(const int32_t* s, int lo, int hi, int32_t key) {
     int end = hi;
@@ -118,32 +140,53 @@ __device__ __forceinline__ int bsearch_i32(const int32_t* s, int lo, int hi, int
     return (lo < end && s[lo] == key) ? lo : -1;
 }
 
-// Per-row state of one staged row (shared memory or, beyond the cap, global).
-template <int M>
+// One staged row.  packed: counters in shared memory, one 32-bit word per
+// entry (accum: count; roles/list: role-A count in the low half, role-B count
+// in the high half); otherwise the global per-edge arrays.
 struct RowState {
     const int32_t* su;            // N+(u)
-    int32_t* cnt0;                // accum: counters; roles: role A counters
-    int32_t* cnt1;                // roles: role B counters
-    unsigned long long* curA;     // list: slot cursors of (u, su[i]) as role A
-    unsigned long long* curB;     // list: slot cursors as role B
+    uint32_t* cnt;
+    const uint32_t* bm;           // bitmap of hashed N+(u)
+    int bm_log2;
+    int d;
+    int32_t umax;                 // largest id in N+(u)
+    bool packed;
     int64_t bu;                   // position of the row's first edge
 };
 
 // One triangle (u, v = su[i], w = su[p]) with (v,w) at position pos.
 template <int M>
-__device__ __forceinline__ void on_triangle(const RowState<M>& R, const SupArgs& A, int i, int p, int64_t pos) {
+__device__ __forceinline__ void on_triangle(const RowState& R, const SupArgs& A, int i, int p, int64_t pos) {
     if (M == kSupAccum) {
-        atomicAdd(R.cnt0 + p, 1);
-        atomicAdd(R.cnt0 + i, 1);
+        if (R.packed) {
+            atomicAdd(R.cnt + i, 1u);
+            atomicAdd(R.cnt + p, 1u);
+        } else {
+            atomicAdd(A.out + R.bu + i, 1);
+            atomicAdd(A.out + R.bu + p, 1);
+        }
         atomicAdd(A.out + pos, 1);
     } else if (M == kSupRoles) {
-        atomicAdd(R.cnt0 + i, 1);
-        atomicAdd(R.cnt1 + p, 1);
+        if (R.packed) {
+            atomicAdd(R.cnt + i, 1u);
+            atomicAdd(R.cnt + p, 1u << 16);
+        } else {
+            atomicAdd(A.cA + R.bu + i, 1);
+            atomicAdd(A.cB + R.bu + p, 1);
+        }
         atomicAdd(A.cC + pos, 1);
     } else {
         const int32_t eA = (int32_t)(R.bu + i), eB = (int32_t)(R.bu + p), eC = (int32_t)pos;
-        const unsigned long long sA = atomicAdd(R.curA + i, 1ull);
-        const unsigned long long sB = atomicAdd(R.curB + p, 1ull);
+        unsigned long long sA, sB;
+        if (R.packed) {
+            const uint32_t a = atomicAdd(R.cnt + i, 1u) & 0xffffu;
+            const uint32_t b = atomicAdd(R.cnt + p, 1u << 16) >> 16;
+            sA = (unsigned long long)__ldg(A.off + eA) + a;
+            sB = (unsigned long long)__ldg(A.off + eB) + (unsigned long long)__ldg(A.cA_in + eB) + b;
+        } else {
+            sA = atomicAdd(A.curA_g + eA, 1ull);
+            sB = atomicAdd(A.curB_g + eB, 1ull);
+        }
         const unsigned long long sC = atomicAdd(A.curC + pos, 1ull);
         A.lists[sA] = make_int2(eB, eC);
         A.lists[sB] = make_int2(eA, eC);
@@ -151,174 +194,168 @@ __device__ __forceinline__ void on_triangle(const RowState<M>& R, const SupArgs&
     }
 }
 
-// One warp processes the v-batches vb = first, first+step, ... of row u.
-// kIdOrdered: every edge goes from a lower to a higher vertex id (the
-// reference's rank orientation), so w lies after v in N+(u) and the last v has
-// no partner; without it (any acyclic orientation) all of N+(u) is searched.
+// Per-warp candidate queue: wedge position (the (v,w) edge) and v's index i.
+struct WarpQueue {
+    int32_t* pos;
+    int32_t* vi;
+    int n;                        // warp-uniform fill
+};
+
+// Resolve queue entries [0, cnt) (cnt <= 32), one per lane.
 template <int M, bool kIdOrdered, class Off>
-__device__ __forceinline__ void wedge_walk(const OutRows<Off>& G, const SupArgs& A, const RowState<M>& R, int d,
-                                           int first, int step, int32_t* s_excl, Off* s_bv) {
+__device__ __forceinline__ void resolve(const OutRows<Off>& G, const SupArgs& A, const RowState& R,
+                                        const WarpQueue& Q, int cnt) {
     const unsigned lane = lane_id();
-    const int32_t* su = R.su;
-    const int32_t umax = su[d - 1];
-    const int vend = kIdOrdered ? d - 1 : d;
-    for (int vb = first; vb < vend; vb += step) {
-        const int i = vb + (int)lane;
-        int32_t len = 0;
-        Off bv = 0;
-        if (i < vend) {
-            int32_t v = su[i];
-            if (v >= 0 && v < G.nv) {
-                bv = G.begin(v);
-                len = (int32_t)(G.end(v) - bv);
-            }
-        }
-        int32_t incl = warp_incl_scan(len);
-        int32_t total = __shfl_sync(kFull, incl, 31);
-        s_excl[lane] = incl - len;
-        s_bv[lane] = bv;
-        __syncwarp();
-        for (int32_t t = lane; t < total; t += kWarp) {
-            // owner lane o: last o with s_excl[o] <= t
-            int lo = 0, hi = 31;
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (s_excl[mid] <= t) lo = mid; else hi = mid - 1;
-            }
-            const int o = lo;
-            const Off pos = s_bv[o] + (t - s_excl[o]);
-            const int32_t w = __ldg(G.cols + pos);
-            if (w > umax) continue;
-            const int p = bsearch_i32(su, kIdOrdered ? vb + o + 1 : 0, d, w);
-            if (p >= 0) on_triangle<M>(R, A, vb + o, p, (int64_t)pos);
-        }
-        __syncwarp();
+    if ((int)lane < cnt) {
+        const int32_t pos = Q.pos[lane];
+        const int i = Q.vi[lane];
+        const int32_t w = __ldg(G.cols + pos);
+        const int p = bsearch_i32(R.su, kIdOrdered ? i + 1 : 0, R.d, w);
+        if (p >= 0) on_triangle<M>(R, A, i, p, (int64_t)pos);
     }
 }
 
-// Stage row u (d entries at bu) into buf; rows that do not fit use global arrays.
-template <int M, class Off>
-__device__ __forceinline__ RowState<M> stage_row(const OutRows<Off>& G, const SupArgs& A, unsigned char* buf,
-                                                 int cap, bool in_smem, Off bu, int d, int tid, int nthr) {
-    RowState<M> R;
-    R.bu = bu;
-    R.cnt0 = R.cnt1 = nullptr;
-    R.curA = R.curB = nullptr;
-    if (!in_smem) {
-        R.su = G.cols + bu;
-        if (M == kSupAccum) R.cnt0 = A.out + bu;
-        if (M == kSupRoles) { R.cnt0 = A.cA + bu; R.cnt1 = A.cB + bu; }
-        if (M == kSupList) { R.curA = A.curA_g + bu; R.curB = A.curB_g + bu; }
-        return R;
+// Walk wedges [w0, w1) of a group: S[0..n) are the strictly increasing starts
+// of the group's non-empty out-lists in the flat wedge space, BV their
+// positions in cols, VI the index of their v in N+(u).  w0 is a multiple of
+// 32 and o0 the group entry that holds wedge w0.
+template <int M, bool kIdOrdered, class Off>
+__device__ __forceinline__ void walk_group(const OutRows<Off>& G, const SupArgs& A, const RowState& R,
+                                           const int32_t* S, const int32_t* VI, const Off* BV, int n, int w0, int w1,
+                                           int o0, WarpQueue& Q) {
+    const unsigned lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    int ob = o0;
+    for (int base = w0; base < w1; base += kWarp) {
+        // group starts inside (base, base + 32): each is > base, and at most 31 fit
+        const int k = ob + 1 + (int)lane;
+        const int32_t B = k < n ? S[k] : INT32_MAX;
+        const unsigned bit = ((unsigned)(B - base) < (unsigned)kWarp) ? (1u << (B - base)) : 0u;
+        const unsigned mk = __reduce_or_sync(kFull, bit);
+        const int nb = __popc(mk);
+        const int32_t Bn = __shfl_sync(kFull, B, nb);
+        const int t = base + (int)lane;
+        bool cand = false;
+        int32_t pos32 = 0;
+        int vi = 0;
+        if (t < w1) {
+            const int o = ob + __popc(mk & (lt | (1u << lane)));
+            const Off pos = BV[o] + (Off)(t - S[o]);
+            const int32_t w = __ldg(G.cols + pos);
+            if (w <= R.umax) {
+                const uint32_t h = bm_hash(w, R.bm_log2);
+                cand = (R.bm[h >> 5] >> (h & 31)) & 1u;
+            }
+            pos32 = (int32_t)pos;
+            vi = VI[o];
+        }
+        ob += nb + (Bn == base + kWarp ? 1 : 0);
+        const unsigned cm = __ballot_sync(kFull, cand);
+        if (cm) {
+            if (cand) {
+                const int at = Q.n + __popc(cm & lt);
+                Q.pos[at] = pos32;
+                Q.vi[at] = vi;
+            }
+            Q.n += __popc(cm);
+            if (Q.n >= kWarp) {
+                __syncwarp();
+                resolve<M, kIdOrdered>(G, A, R, Q, kWarp);
+                __syncwarp();
+                const int rest = Q.n - kWarp;
+                int32_t p2 = 0, v2 = 0;
+                if ((int)lane < rest) {
+                    p2 = Q.pos[kWarp + lane];
+                    v2 = Q.vi[kWarp + lane];
+                }
+                __syncwarp();
+                if ((int)lane < rest) {
+                    Q.pos[lane] = p2;
+                    Q.vi[lane] = v2;
+                }
+                __syncwarp();
+                Q.n = rest;
+            }
+        }
     }
-    int32_t* su = reinterpret_cast<int32_t*>(buf);
-    R.su = su;
-    if (M == kSupList) {
-        unsigned long long* ca = reinterpret_cast<unsigned long long*>(buf + ((4 * cap + 15) & ~15));
-        unsigned long long* cb = ca + cap;
-        R.curA = ca;
-        R.curB = cb;
+}
+
+template <int M, bool kIdOrdered, class Off>
+__device__ __forceinline__ void drain(const OutRows<Off>& G, const SupArgs& A, const RowState& R, WarpQueue& Q) {
+    __syncwarp();
+    if (Q.n > 0) resolve<M, kIdOrdered>(G, A, R, Q, Q.n);
+    __syncwarp();
+    Q.n = 0;
+}
+
+// Stage row u (d entries at bu).  in_smem: su and packed counters in the
+// given buffers; otherwise the global arrays.  The bitmap (2^bm_log2 bits) is
+// cleared and filled; block_sync selects block- or warp-wide synchronisation.
+template <int M, class Off>
+__device__ __forceinline__ RowState stage_row(const OutRows<Off>& G, const SupArgs& A, int32_t* su_buf,
+                                              uint32_t* cnt_buf, uint32_t* bm, int bm_log2, bool in_smem, Off bu,
+                                              int d, int tid, int nthr, bool block_sync) {
+    RowState R;
+    R.bu = bu;
+    R.d = d;
+    R.bm = bm;
+    R.bm_log2 = bm_log2;
+    R.packed = in_smem;
+    for (int i = tid; i < (1 << bm_log2) / 32; i += nthr) bm[i] = 0u;
+    if (block_sync) __syncthreads(); else __syncwarp();
+    if (in_smem) {
+        R.su = su_buf;
+        R.cnt = cnt_buf;
         for (int i = tid; i < d; i += nthr) {
-            su[i] = __ldg(G.cols + bu + i);
-            const unsigned long long o = (unsigned long long)__ldg(A.off + bu + i);
-            ca[i] = o;
-            cb[i] = o + (unsigned long long)__ldg(A.cA_in + bu + i);
+            const int32_t w = __ldg(G.cols + bu + i);
+            su_buf[i] = w;
+            cnt_buf[i] = 0u;
+            const uint32_t h = bm_hash(w, bm_log2);
+            atomicOr(bm + (h >> 5), 1u << (h & 31));
         }
     } else {
-        int32_t* c0 = su + cap;
-        int32_t* c1 = c0 + cap;
-        R.cnt0 = c0;
-        R.cnt1 = c1;
+        R.su = G.cols + bu;
+        R.cnt = nullptr;
         for (int i = tid; i < d; i += nthr) {
-            su[i] = __ldg(G.cols + bu + i);
-            c0[i] = 0;
-            if (M == kSupRoles) c1[i] = 0;
+            const uint32_t h = bm_hash(__ldg(G.cols + bu + i), bm_log2);
+            atomicOr(bm + (h >> 5), 1u << (h & 31));
         }
     }
+    R.umax = d > 0 ? __ldg(G.cols + bu + d - 1) : INT32_MIN;
     return R;
 }
 
-// Heavy rows in shared memory: the row's (v, w) pair space is flattened with
-// a block-wide prefix over d+(v) so every thread gets an equal share of the
-// pairs (a row's pairs can be far more than 32 lanes x d).
-template <int M, bool kIdOrdered, class Off>
-__device__ __forceinline__ void heavy_flat_walk(const OutRows<Off>& G, const SupArgs& A, const RowState<M>& R, int d,
-                                                int32_t* pre, Off* bv, int32_t* s_wsum) {
-    const int tid = threadIdx.x;
-    const unsigned lane = lane_id();
-    const int wib = tid / kWarp;
-    const int32_t* su = R.su;
-    const int vend = kIdOrdered ? d - 1 : d;
-    // pre[i] = sum of d+(su[j]) for j < i, for i in [0, vend]
-    int32_t carry = 0;
-    for (int base = 0; base < vend; base += kSupBlock) {
-        const int i = base + tid;
-        int32_t len = 0;
-        Off b = 0;
-        if (i < vend) {
-            const int32_t v = su[i];
-            if (v >= 0 && v < G.nv) {
-                b = G.begin(v);
-                len = (int32_t)(G.end(v) - b);
-            }
-            bv[i] = b;
-        }
-        int32_t incl = warp_incl_scan(len);
-        if (lane == 31) s_wsum[wib] = incl;
-        __syncthreads();
-        if (wib == 0) {
-            int32_t x = s_wsum[lane < kSupWarps ? lane : 0];
-            if (lane >= kSupWarps) x = 0;
-            const int32_t xi = warp_incl_scan(x);
-            if (lane < kSupWarps) s_wsum[lane] = xi - x;
-            if (lane == kSupWarps - 1) s_wsum[kSupWarps] = xi;
-        }
-        __syncthreads();
-        if (i < vend) pre[i] = carry + s_wsum[wib] + incl - len;
-        carry += s_wsum[kSupWarps];
-        __syncthreads();
-    }
-    if (tid == 0) pre[vend] = carry;
-    __syncthreads();
-    const int32_t total = carry;
-    const int32_t umax = su[d - 1];
-    for (int32_t t = tid; t < total; t += kSupBlock) {
-        int lo = 0, hi = vend - 1;  // last i with pre[i] <= t
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (pre[mid] <= t) lo = mid; else hi = mid - 1;
-        }
-        const Off pos = bv[lo] + (t - pre[lo]);
-        const int32_t w = __ldg(G.cols + pos);
-        if (w > umax) continue;
-        const int p = bsearch_i32(su, kIdOrdered ? lo + 1 : 0, d, w);
-        if (p >= 0) on_triangle<M>(R, A, lo, p, (int64_t)pos);
-    }
-}
-
 template <int M>
-__device__ __forceinline__ void flush_row(const RowState<M>& R, const SupArgs& A, bool in_smem, int d, int tid,
-                                          int nthr) {
+__device__ __forceinline__ void flush_row(const RowState& R, const SupArgs& A, int tid, int nthr) {
+    const int d = R.d;
     if (M == kSupList) {
-        // every role-A / role-B cursor of the row must have reached the end of
-        // its segment: the listing pass found exactly the triangles counted
+        // every role-A / role-B counter of the row must have reached its count:
+        // the listing pass found exactly the triangles the support pass counted
         for (int i = tid; i < d; i += nthr) {
-            const unsigned long long o = (unsigned long long)__ldg(A.off + R.bu + i);
-            const unsigned long long a = o + (unsigned long long)__ldg(A.cA_in + R.bu + i);
-            const unsigned long long b = a + (unsigned long long)__ldg(A.cB_in + R.bu + i);
-            if ((R.curA[i] != a || R.curB[i] != b) && A.status) atomicMax(A.status, (int)TDT_ERR_CAPACITY);
+            const int64_t e = R.bu + i;
+            const uint32_t ca = (uint32_t)__ldg(A.cA_in + e), cb = (uint32_t)__ldg(A.cB_in + e);
+            bool bad;
+            if (R.packed) {
+                const uint32_t c = R.cnt[i];
+                bad = (c & 0xffffu) != ca || (c >> 16) != cb;
+            } else {
+                const unsigned long long o = (unsigned long long)__ldg(A.off + e);
+                bad = A.curA_g[e] != o + ca || A.curB_g[e] != o + ca + cb;
+            }
+            if (bad && A.status) atomicMax(A.status, (int)TDT_ERR_CAPACITY);
         }
         return;
     }
-    if (!in_smem) return;
+    if (!R.packed) return;
     if (M == kSupAccum) {
         for (int i = tid; i < d; i += nthr)
-            if (R.cnt0[i]) atomicAdd(A.out + R.bu + i, R.cnt0[i]);
-    } else if (M == kSupRoles) {
+            if (R.cnt[i]) atomicAdd(A.out + R.bu + i, (int32_t)R.cnt[i]);
+    } else {
         // role A/B counts of row u's edges come only from row u: plain stores
         for (int i = tid; i < d; i += nthr) {
-            A.cA[R.bu + i] = R.cnt0[i];
-            A.cB[R.bu + i] = R.cnt1[i];
+            const uint32_t c = R.cnt[i];
+            A.cA[R.bu + i] = (int32_t)(c & 0xffffu);
+            A.cB[R.bu + i] = (int32_t)(c >> 16);
         }
     }
 }
@@ -326,12 +363,10 @@ __device__ __forceinline__ void flush_row(const RowState<M>& R, const SupArgs& A
 // ctl != nullptr: dynamic scheduling through its counters (zeroed by the
 // caller); ctl == nullptr: static round-robin scheduling (no scratch at all).
 template <int M, bool kIdOrdered, class Off>
-__global__ void __launch_bounds__(kSupBlock) support_kernel(OutRows<Off> G, SupArgs A, SupCtl* ctl) {
+__global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRows<Off> G, SupArgs A, SupCtl* ctl) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int32_t s_excl[kSupWarps][kWarp];
-    __shared__ Off s_bv[kSupWarps][kWarp];
     __shared__ int32_t s_list[kHeavyChunk];
-    __shared__ int32_t s_wsum[kSupWarps + 1];
+    __shared__ int32_t s_wsum[2][kSupWarps + 1];
     __shared__ int s_n;
     __shared__ long long s_chunk;
     const int wib = threadIdx.x / kWarp;
@@ -339,51 +374,127 @@ __global__ void __launch_bounds__(kSupBlock) support_kernel(OutRows<Off> G, SupA
     const int64_t nv = G.nv;
     const long long nchunks = (nv + kHeavyChunk - 1) / kHeavyChunk;
     if (A.gate && *(volatile const int*)A.gate != 0) return;
-    constexpr int kHeavy = HeavyCap<M>::value;
     const int warp_cap = A.warp_cap;
     const int heavy_cap = A.heavy_cap;
 
-    // ---- phase 1: rows with d+(u) > kWarpCap, one block per row
-    for (long long it = 0;; it++) {
-        if (threadIdx.x == 0) {
-            s_chunk = ctl ? (long long)atomicAdd(&ctl->heavy_next, 1ull) : blockIdx.x + it * gridDim.x;
-            s_n = 0;
-        }
-        __syncthreads();
-        const long long c = s_chunk;
-        if (c >= nchunks) break;
-        for (int k = threadIdx.x; k < kHeavyChunk; k += kSupBlock) {
-            const long long u = c * kHeavyChunk + k;
-            if (u < nv && G.end(u) - G.begin(u) > warp_cap) s_list[atomicAdd(&s_n, 1)] = (int32_t)u;
-        }
-        __syncthreads();
-        const int nh = s_n;
-        __syncthreads();  // every thread has read s_n before thread 0 resets it
-        for (int h = 0; h < nh; h++) {
-            const long long u = s_list[h];
-            const Off bu = G.begin(u);
-            const int d = (int)(G.end(u) - bu);
-            const bool in_smem = d <= heavy_cap;
-            RowState<M> R = stage_row<M>(G, A, smem, kHeavy, in_smem, bu, d, threadIdx.x, kSupBlock);
-            __syncthreads();
-            if (in_smem) {
-                // prefix and out-list starts live after the row buffers
-                unsigned char* tail = smem + ((size_t)RowBytes<M>::value * kHeavy + 15) / 16 * 16;
-                Off* bvv = reinterpret_cast<Off*>(tail);
-                int32_t* pre = reinterpret_cast<int32_t*>(bvv + kHeavy);
-                heavy_flat_walk<M, kIdOrdered>(G, A, R, d, pre, bvv, s_wsum);
-            } else {
-                wedge_walk<M, kIdOrdered>(G, A, R, d, wib * kWarp, kSupBlock, s_excl[wib], s_bv[wib]);
+    // ---- phase 1: rows with d+(u) > warp_cap, one block per row
+    {
+        int32_t* h_su = reinterpret_cast<int32_t*>(smem);
+        uint32_t* h_cnt = reinterpret_cast<uint32_t*>(smem + 4 * kHeavyCap);
+        int32_t* g_S = reinterpret_cast<int32_t*>(smem + kHvS);
+        int32_t* g_VI = reinterpret_cast<int32_t*>(smem + kHvVI);
+        Off* g_BV = reinterpret_cast<Off*>(smem + kHvBV);
+        WarpQueue Q;
+        Q.pos = reinterpret_cast<int32_t*>(smem + kHvQueues + wib * 8 * kQueue);
+        Q.vi = Q.pos + kQueue;
+        Q.n = 0;
+        for (long long it = 0;; it++) {
+            if (threadIdx.x == 0) {
+                s_chunk = ctl ? (long long)atomicAdd(&ctl->heavy_next, 1ull) : blockIdx.x + it * gridDim.x;
+                s_n = 0;
             }
             __syncthreads();
-            flush_row<M>(R, A, in_smem, d, threadIdx.x, kSupBlock);
+            const long long c = s_chunk;
+            if (c >= nchunks) break;
+            for (int k = threadIdx.x; k < kHeavyChunk; k += kSupBlock) {
+                const long long u = c * kHeavyChunk + k;
+                if (u < nv && G.end(u) - G.begin(u) > warp_cap) s_list[atomicAdd(&s_n, 1)] = (int32_t)u;
+            }
             __syncthreads();
+            const int nh = s_n;
+            __syncthreads();  // every thread has read s_n before thread 0 resets it
+            for (int h = 0; h < nh; h++) {
+                const long long u = s_list[h];
+                const Off bu = G.begin(u);
+                const int d = (int)(G.end(u) - bu);
+                const bool in_smem = d <= heavy_cap;
+                uint32_t* bm = in_smem ? reinterpret_cast<uint32_t*>(smem + kHvBm) : reinterpret_cast<uint32_t*>(smem);
+                RowState R = stage_row<M>(G, A, h_su, h_cnt, bm, in_smem ? kHeavyBmLog2 : kHugeBmLog2, in_smem, bu, d,
+                                          threadIdx.x, kSupBlock, true);
+                __syncthreads();
+                const int vend = kIdOrdered ? d - 1 : d;
+                for (int g0 = 0; g0 < vend; g0 += kSeg) {
+                    // group: v's g0 .. g0+511, one per thread
+                    const int i = g0 + threadIdx.x;
+                    int32_t len = 0;
+                    Off bv = 0;
+                    if (i < vend) {
+                        const int32_t v = R.su[i];
+                        if (v >= 0 && v < nv) {
+                            bv = G.begin(v);
+                            len = (int32_t)(G.end(v) - bv);
+                        }
+                    }
+                    const unsigned nem = __ballot_sync(kFull, len > 0);
+                    const int32_t incl = warp_incl_scan(len);
+                    if (lane == 31) {
+                        s_wsum[0][wib] = incl;
+                        s_wsum[1][wib] = __popc(nem);
+                    }
+                    __syncthreads();
+                    if (wib == 0) {
+                        const int32_t x = (int)lane < kSupWarps ? s_wsum[0][lane] : 0;
+                        const int32_t y = (int)lane < kSupWarps ? s_wsum[1][lane] : 0;
+                        const int32_t xi = warp_incl_scan(x), yi = warp_incl_scan(y);
+                        if ((int)lane < kSupWarps) {
+                            s_wsum[0][lane] = xi - x;
+                            s_wsum[1][lane] = yi - y;
+                        }
+                        if ((int)lane == kSupWarps - 1) {
+                            s_wsum[0][kSupWarps] = xi;
+                            s_wsum[1][kSupWarps] = yi;
+                        }
+                    }
+                    __syncthreads();
+                    if (len > 0) {
+                        const int ci = s_wsum[1][wib] + __popc(nem & lanemask_lt());
+                        g_S[ci] = s_wsum[0][wib] + incl - len;
+                        g_VI[ci] = i;
+                        g_BV[ci] = bv;
+                    }
+                    const int total = s_wsum[0][kSupWarps];
+                    const int n = s_wsum[1][kSupWarps];
+                    __syncthreads();
+                    // equal shares of the group's wedges, in whole steps of 32
+                    const int share = ((total + kSupBlock - 1) / kSupBlock) * kWarp;
+                    const int w0 = wib * share;
+                    const int w1 = w0 + share < total ? w0 + share : total;
+                    if (w0 < w1) {
+                        int o0 = 0;
+                        if (lane == 0) {
+                            int lo = 0, hi = n - 1;  // last entry with S <= w0
+                            while (lo < hi) {
+                                const int mid = (lo + hi + 1) >> 1;
+                                if (g_S[mid] <= w0) lo = mid; else hi = mid - 1;
+                            }
+                            o0 = lo;
+                        }
+                        o0 = __shfl_sync(kFull, o0, 0);
+                        walk_group<M, kIdOrdered>(G, A, R, g_S, g_VI, g_BV, n, w0, w1, o0, Q);
+                    }
+                    __syncthreads();  // the group arrays are rewritten next
+                }
+                drain<M, kIdOrdered>(G, A, R, Q);
+                __syncthreads();
+                flush_row<M>(R, A, threadIdx.x, kSupBlock);
+                __syncthreads();
+            }
         }
     }
 
-    // ---- phase 2: rows with 2 <= d+(u) <= kWarpCap, one warp per row, taken
+    // ---- phase 2: rows with 2 <= d+(u) <= warp_cap, one warp per row, taken
     // in batches from the top ids (highest degree rank) down
-    unsigned char* wbuf = smem + wib * (RowBytes<M>::value * WarpCap<M>::value);
+    unsigned char* sl = smem + wib * kSliceBytes;
+    int32_t* l_su = reinterpret_cast<int32_t*>(sl + kSlSu);
+    uint32_t* l_cnt = reinterpret_cast<uint32_t*>(sl + kSlCnt);
+    int32_t* l_S = reinterpret_cast<int32_t*>(sl + kSlS);
+    int32_t* l_VI = reinterpret_cast<int32_t*>(sl + kSlVI);
+    Off* l_BV = reinterpret_cast<Off*>(sl + kSlBV);
+    uint32_t* l_bm = reinterpret_cast<uint32_t*>(sl + kSlBm);
+    WarpQueue Q;
+    Q.pos = reinterpret_cast<int32_t*>(sl + kSlQ);
+    Q.vi = Q.pos + kQueue;
+    Q.n = 0;
     const long long gw = (long long)blockIdx.x * kSupWarps + wib;
     const long long nw = (long long)gridDim.x * kSupWarps;
     for (long long it = 0;; it++) {
@@ -401,11 +512,35 @@ __global__ void __launch_bounds__(kSupBlock) support_kernel(OutRows<Off> G, SupA
             const Off bu = G.begin(uu);
             const int d = (int)(G.end(uu) - bu);
             if (d < 2 || d > warp_cap) continue;
-            RowState<M> R = stage_row<M>(G, A, wbuf, WarpCap<M>::value, true, bu, d, lane, kWarp);
+            RowState R = stage_row<M>(G, A, l_su, l_cnt, l_bm, kLightBmLog2, true, bu, d, lane, kWarp, false);
             __syncwarp();
-            wedge_walk<M, kIdOrdered>(G, A, R, d, 0, kWarp, s_excl[wib], s_bv[wib]);
-            __syncwarp();
-            flush_row<M>(R, A, true, d, lane, kWarp);
+            const int vend = kIdOrdered ? d - 1 : d;
+            for (int vb = 0; vb < vend; vb += kWarp) {
+                const int i = vb + (int)lane;
+                int32_t len = 0;
+                Off bv = 0;
+                if (i < vend) {
+                    const int32_t v = l_su[i];
+                    if (v >= 0 && v < nv) {
+                        bv = G.begin(v);
+                        len = (int32_t)(G.end(v) - bv);
+                    }
+                }
+                const unsigned nem = __ballot_sync(kFull, len > 0);
+                const int32_t incl = warp_incl_scan(len);
+                const int total = __shfl_sync(kFull, incl, 31);
+                if (len > 0) {
+                    const int ci = __popc(nem & lanemask_lt());
+                    l_S[ci] = incl - len;
+                    l_VI[ci] = i;
+                    l_BV[ci] = bv;
+                }
+                __syncwarp();
+                if (total > 0) walk_group<M, kIdOrdered>(G, A, R, l_S, l_VI, l_BV, __popc(nem), 0, total, 0, Q);
+                __syncwarp();
+            }
+            drain<M, kIdOrdered>(G, A, R, Q);
+            flush_row<M>(R, A, lane, kWarp);
             __syncwarp();
         }
     }
@@ -417,8 +552,8 @@ static int launch_mode(const OutRows<Off>& G, const SupArgs& A, SupCtl* ctl, cud
     int rc = device_info(&di);
     if (rc) return rc;
     SupArgs A2 = A;
-    A2.warp_cap = (g_warp_cap > 0 && g_warp_cap < WarpCap<M>::value) ? g_warp_cap : WarpCap<M>::value;
-    A2.heavy_cap = (g_heavy_cap > 0 && g_heavy_cap < HeavyCap<M>::value) ? g_heavy_cap : HeavyCap<M>::value;
+    A2.warp_cap = (g_warp_cap > 0 && g_warp_cap < kWarpCap) ? g_warp_cap : kWarpCap;
+    A2.heavy_cap = (g_heavy_cap > 0 && g_heavy_cap < kHeavyCap) ? g_heavy_cap : kHeavyCap;
     auto kern = support_kernel<M, kIdOrdered, Off>;
     TDT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSupSmemBytes));
     TDT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
