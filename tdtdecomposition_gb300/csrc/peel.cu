@@ -95,6 +95,46 @@ __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long
     return __ldcg(p);
 }
 
+// Queue item of edge e (listed: e's list offset and length; search: the
+// lower-degree endpoint x, the other endpoint y, x's out-degree dxo and the
+// candidate count dx).  Returns false when e has nothing to enumerate.
+template <bool Listed>
+__device__ __forceinline__ bool make_item(const PeelArgs& A, bool want, int32_t cur_sup, int32_t e, int4& it,
+                                          long long& dx) {
+    it = make_int4(e, 0, 0, 0);
+    dx = 0;
+    if (!want || cur_sup <= 0) return false;
+    if (Listed) {
+        // the edge's original triangles; the item carries the list offset
+        const long long o = __ldg(A.off + e);
+        dx = __ldg(A.off + e + 1) - o;
+        it.y = (int32_t)(unsigned)(o & 0xffffffffll);
+        it.z = (int32_t)(o >> 32);
+        return dx > 0;
+    }
+    const int32_t u = __ldg(A.rows + e), v = __ldg(A.cols + e);
+    const long long duo = __ldg(A.rp + u + 1) - __ldg(A.rp + u);
+    const long long du = duo + __ldg(A.cp + u + 1) - __ldg(A.cp + u);
+    const long long dvo = __ldg(A.rp + v + 1) - __ldg(A.rp + v);
+    const long long dv = dvo + __ldg(A.cp + v + 1) - __ldg(A.cp + v);
+    if (du <= dv) { it.y = u; it.z = v; dx = du; it.w = (int32_t)duo; }
+    else { it.y = v; it.z = u; dx = dv; it.w = (int32_t)dvo; }
+    return dx > 1;
+}
+
+// Reserve n items and tot candidate slots of the round in `slot` (lane 0's
+// atomic, broadcast); sets TDT_ERR_CAPACITY past the queue limits.
+__device__ __forceinline__ unsigned long long reserve_items(const PeelArgs& A, int slot, int n, long long tot) {
+    unsigned long long old = 0;
+    if (lane_id() == 0) {
+        old = atomicAdd(&A.ctl->q[slot], ((unsigned long long)n << kCandBits) + (unsigned long long)tot);
+        const unsigned long long it0 = old >> kCandBits, c0 = old & kCandMask;
+        if (it0 + n >= (1ull << kItemBits) || c0 + tot >= (1ull << kCandBits) || (long long)(it0 + n) > A.E)
+            set_status(A.ctl, TDT_ERR_CAPACITY);
+    }
+    return __shfl_sync(kFull, old, 0);
+}
+
 // Queue the edges flagged by `want` (one per lane) for the round in `slot`
 // and add their number to *nfront.  cur_sup is the edge's support at marking
 // time (0 => no alive triangle).
@@ -104,47 +144,59 @@ __device__ __forceinline__ void warp_append(const PeelArgs& A, int slot, int buf
     const unsigned mf = __ballot_sync(kFull, want);
     if (mf == 0) return;
     if (lane == (unsigned)(__ffs(mf) - 1)) atomicAdd(nfront, (unsigned long long)__popc(mf));
-    int32_t x = 0, y = 0, dxo = 0;
-    long long dx = 0;
-    bool q = want && cur_sup > 0;
-    if (q && A.lists) {
-        // the edge's original triangles; the item carries the list offset
-        const long long o = __ldg(A.off + e);
-        dx = __ldg(A.off + e + 1) - o;
-        x = (int32_t)(unsigned)(o & 0xffffffffll);
-        y = (int32_t)(o >> 32);
-        if (dx <= 0) q = false;
-    } else if (q) {
-        const int32_t u = __ldg(A.rows + e), v = __ldg(A.cols + e);
-        const long long duo = __ldg(A.rp + u + 1) - __ldg(A.rp + u);
-        const long long du = duo + __ldg(A.cp + u + 1) - __ldg(A.cp + u);
-        const long long dvo = __ldg(A.rp + v + 1) - __ldg(A.rp + v);
-        const long long dv = dvo + __ldg(A.cp + v + 1) - __ldg(A.cp + v);
-        if (du <= dv) { x = u; y = v; dx = du; dxo = (int32_t)duo; }
-        else { x = v; y = u; dx = dv; dxo = (int32_t)dvo; }
-        if (dx <= 1) q = false;
-    }
+    int4 it;
+    long long dx;
+    const bool q = A.lists ? make_item<true>(A, want, cur_sup, e, it, dx) : make_item<false>(A, want, cur_sup, e, it, dx);
     const unsigned m = __ballot_sync(kFull, q);
     if (m == 0) return;
     const long long c = q ? dx : 0;
     const long long incl = warp_incl_scan(c);
     const long long tot = __shfl_sync(kFull, incl, 31);
-    const int n = __popc(m);
-    unsigned long long old = 0;
-    if (lane == 0) {
-        old = atomicAdd(&A.ctl->q[slot], ((unsigned long long)n << kCandBits) + (unsigned long long)tot);
-        const unsigned long long it0 = old >> kCandBits, c0 = old & kCandMask;
-        if (it0 + n >= (1ull << kItemBits) || c0 + tot >= (1ull << kCandBits) || (long long)(it0 + n) > A.E)
-            set_status(A.ctl, TDT_ERR_CAPACITY);
-    }
-    old = __shfl_sync(kFull, old, 0);
+    const unsigned long long old = reserve_items(A, slot, __popc(m), tot);
     if (q) {
         const long long it0 = (long long)(old >> kCandBits), c0 = (long long)(old & kCandMask);
         const long long idx = it0 + __popc(m & lanemask_lt());
         if (idx < A.E) {
-            A.qi[buf][idx] = make_int4(e, x, y, dxo);
+            A.qi[buf][idx] = it;
             A.qb[buf][idx] = c0 + incl - c;
         }
+    }
+}
+
+// The same for up to two edges per lane (f, g of one triangle), with one
+// reservation for the warp.
+template <bool Listed>
+__device__ __forceinline__ void warp_append2(const PeelArgs& A, int slot, int buf, bool wf, int32_t f, bool wg,
+                                             int32_t g, int32_t cur_sup, unsigned long long* nfront) {
+    const unsigned lane = lane_id();
+    const unsigned mf = __ballot_sync(kFull, wf), mg = __ballot_sync(kFull, wg);
+    if ((mf | mg) == 0) return;
+    if (lane == 0) atomicAdd(nfront, (unsigned long long)(__popc(mf) + __popc(mg)));
+    int4 itf, itg;
+    long long dxf, dxg;
+    const bool qf = make_item<Listed>(A, wf, cur_sup, f, itf, dxf);
+    const bool qg = make_item<Listed>(A, wg, cur_sup, g, itg, dxg);
+    const int nq = (qf ? 1 : 0) + (qg ? 1 : 0);
+    if (__ballot_sync(kFull, nq > 0) == 0) return;
+    const long long c = (qf ? dxf : 0) + (qg ? dxg : 0);
+    const int nincl = warp_incl_scan(nq);
+    const long long cincl = warp_incl_scan(c);
+    const int ntot = __shfl_sync(kFull, nincl, 31);
+    const long long ctot = __shfl_sync(kFull, cincl, 31);
+    const unsigned long long old = reserve_items(A, slot, ntot, ctot);
+    long long idx = (long long)(old >> kCandBits) + nincl - nq;
+    long long cc = (long long)(old & kCandMask) + cincl - c;
+    if (qf) {
+        if (idx < A.E) {
+            A.qi[buf][idx] = itf;
+            A.qb[buf][idx] = cc;
+        }
+        idx++;
+        cc += dxf;
+    }
+    if (qg && idx < A.E) {
+        A.qi[buf][idx] = itg;
+        A.qb[buf][idx] = cc;
     }
 }
 
@@ -364,10 +416,13 @@ __device__ bool fixed_start(const PeelArgs& A, int32_t l) {
 
 // One sub-round: warps gwarp = 0..nwarps-1 share the candidate slots of round r.
 // The smallest decrement result above l is folded into *dmin (the lower bound
-// of the next level).
-__device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp,
-                                              long long nwarps, long long* s_win, int* dmin) {
+// of the next level).  Compiled once per mode and not inlined, so its
+// registers are allocated apart from the persistent loop around it.
+template <bool Listed>
+__device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp, long long nwarps,
+                                           int* dmin) {
     const unsigned lane = lane_id();
+    const unsigned le = lanemask_lt() | (1u << lane);
     int32_t dm = INT32_MAX;
     const int slot = r % 3, buf = r & 1;
     const int nslot = (r + 1) % 3, nbuf = buf ^ 1;
@@ -376,114 +431,98 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     const long long T = (long long)(packed & kCandMask);
     const long long* __restrict__ qb = A.qb[buf];
     const int4* __restrict__ qi = A.qi[buf];
-    // each warp owns a contiguous range of candidate slots; the owning item
-    // of its first slot is found once, later ones by sliding the window
+    // each warp owns a contiguous range of candidate slots; the item of its
+    // first slot is found once by binary search, later ones step by step
     const long long per_warp = (((T + nwarps - 1) / nwarps) + 31) & ~31ll;
     const long long cb0 = gwarp * per_warp;
     const long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
+    if (cb0 >= cb1) return;
     long long i0 = 0;
-    if (cb0 < cb1) {
-        if (lane == 0) {
-            long long lo = 0, hi = N - 1;
-            while (lo < hi) {
-                long long mid = (lo + hi + 1) >> 1;
-                if (__ldcg(qb + mid) <= cb0) lo = mid; else hi = mid - 1;
-            }
-            i0 = lo;
+    if (lane == 0) {
+        long long lo = 0, hi = N - 1;
+        while (lo < hi) {
+            long long mid = (lo + hi + 1) >> 1;
+            if (__ldcg(qb + mid) <= cb0) lo = mid; else hi = mid - 1;
         }
-        i0 = __shfl_sync(kFull, i0, 0);
+        i0 = lo;
     }
+    i0 = __shfl_sync(kFull, i0, 0);
+    long long base0 = __ldcg(qb + i0);  // first slot of item i0 (<= cb)
     for (long long cb = cb0; cb < cb1; cb += kWarp) {
-        s_win[lane] = (i0 + lane < N) ? __ldcg(qb + i0 + lane) : LLONG_MAX;
-        __syncwarp();
+        // item i0 holds slot cb; items i0+1.. start at B (strictly increasing,
+        // all > cb), so the starts inside (cb, cb+32) are at most 31
+        const long long B = (i0 + 1 + lane < N) ? __ldcg(qb + i0 + 1 + lane) : LLONG_MAX;
+        const unsigned bit = (B - cb < kWarp) ? (1u << (unsigned)(B - cb)) : 0u;
+        const unsigned mk = __reduce_or_sync(kFull, bit);
+        const int k = __popc(mk & le);          // this lane's item is i0 + k
+        const long long Bk = __shfl_sync(kFull, B, (k + 31) & 31);
+        const long long base_l = k == 0 ? base0 : Bk;
+        const int nb = __popc(mk);
+        const long long Bn = __shfl_sync(kFull, B, nb);
+        const long long Bl = __shfl_sync(kFull, B, (nb + 31) & 31);
         const long long t = cb + lane;
         bool want_f = false, want_g = false;
-        int64_t f = 0, g = 0;
-        // window index of this lane's item: slot cb lies in item i0 and each
-        // item owns >= 1 slot, so slot cb+k lies in item i0+k at most; the
-        // window holds i0..i0+31, and i0+32 is checked with one more load
-        int jl = 0;
-        long long base_l = 0;
-        {
-            int lo = 0, hi = 31;
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (s_win[mid] <= t) lo = mid; else hi = mid - 1;
-            }
-            jl = lo;
-            base_l = s_win[lo];
-            if (lo == 31 && i0 + 32 < N) {
-                const long long nb = __ldcg(qb + i0 + 32);
-                if (nb <= t) { jl = 32; base_l = nb; }
-            }
-        }
+        int32_t f = 0, g = 0;
         if (t < cb1) {
-            const int lo = jl;
-            const long long item = i0 + lo;
-            const int4 it = __ldcg(qi + item);
+            const int4 it = __ldcg(qi + i0 + k);
             const int32_t e = it.x, x = it.y, y = it.z, dxo = it.w;
             const long long tl = t - base_l;
-            int32_t w = y;
-            if (A.lists) {
-                // listed mode: the slot is one of e's triangles, (f, g) its other edges
+            bool tri;
+            if (Listed) {
+                // the slot is one of e's triangles, (f, g) its other edges
                 const long long lo = (long long)(unsigned)x | ((long long)y << 32);
                 const int2 fg = __ldg(A.lists + lo + tl);
                 f = fg.x;
                 g = fg.y;
-                w = ~y;  // any value != y
-            } else if (tl < dxo) {
-                f = __ldg(A.rp + x) + tl;
-                w = __ldg(A.cols + f);
+                tri = true;
             } else {
-                const int64_t k = __ldg(A.cp + x) + (tl - dxo);
-                w = __ldg(A.in_src + k);
-                f = __ldg(A.in_eid + k);
+                int32_t w;
+                if (tl < dxo) {
+                    f = (int32_t)(__ldg(A.rp + x) + tl);
+                    w = __ldg(A.cols + f);
+                } else {
+                    const int64_t kk = __ldg(A.cp + x) + (tl - dxo);
+                    w = __ldg(A.in_src + kk);
+                    f = __ldg(A.in_eid + kk);
+                }
+                tri = w != y;
+                if (tri) {
+                    const int64_t gg = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
+                                               : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
+                    tri = gg >= 0;
+                    g = (int32_t)gg;
+                }
             }
-            if (w != y) {
-                if (!A.lists)
-                    g = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
-                                : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
-                if (g >= 0) {
-                    const int32_t rf = __ldcg(&A.es[f].y), rg = __ldcg(&A.es[g].y);
-                    const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
-                    if (af && ag) {
-                        const bool ff = rf == r, fg = rg == r;
-                        // which of f, g this lane decrements (ownership rules above)
-                        const bool df = !ff && (!fg || e < g);
-                        const bool dg = !fg && (!ff || e < f);
-                        // issue both atomics before using either result
-                        int32_t of = 0, og = 0;
-                        if (df) of = atomicSub(&A.es[f].x, 1);
-                        if (dg) og = atomicSub(&A.es[g].x, 1);
-                        want_f = df && of == l + 1;
-                        want_g = dg && og == l + 1;
-                        if (df && of > l + 1) dm = of - 1 < dm ? of - 1 : dm;
-                        if (dg && og > l + 1) dm = og - 1 < dm ? og - 1 : dm;
-                        if (want_f) A.es[f].y = r + 1;
-                        if (want_g) A.es[g].y = r + 1;
-                    }
+            if (tri) {
+                const int32_t rf = __ldcg(&A.es[f].y), rg = __ldcg(&A.es[g].y);
+                const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
+                if (af && ag) {
+                    const bool ff = rf == r, fg = rg == r;
+                    // which of f, g this lane decrements (ownership rules above)
+                    const bool df = !ff && (!fg || e < g);
+                    const bool dg = !fg && (!ff || e < f);
+                    // issue both atomics before using either result
+                    int32_t of = 0, og = 0;
+                    if (df) of = atomicSub(&A.es[f].x, 1);
+                    if (dg) og = atomicSub(&A.es[g].x, 1);
+                    want_f = df && of == l + 1;
+                    want_g = dg && og == l + 1;
+                    if (df && of > l + 1) dm = of - 1 < dm ? of - 1 : dm;
+                    if (dg && og > l + 1) dm = og - 1 < dm ? og - 1 : dm;
+                    if (want_f) A.es[f].y = r + 1;
+                    if (want_g) A.es[g].y = r + 1;
                 }
             }
         }
-        warp_append(A, nslot, nbuf, want_f, (int32_t)f, l, &A.ctl->fe[nslot]);
-        warp_append(A, nslot, nbuf, want_g, (int32_t)g, l, &A.ctl->fe[nslot]);
-
-        {
-            // the next window starts at the item of slot cb+32 (<= i0+32)
-            int jn = 0;
-            if (lane == 31) {
-                const long long tn = cb + kWarp;
-                int lo = 0, hi = 31;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (s_win[mid] <= tn) lo = mid; else hi = mid - 1;
-                }
-                jn = lo;
-                if (lo == 31 && i0 + 32 < N && __ldcg(qb + i0 + 32) <= tn) jn = 32;
-            }
-            i0 += __shfl_sync(kFull, jn, 31);
+        warp_append2<Listed>(A, nslot, nbuf, want_f, f, want_g, g, l, &A.ctl->fe[nslot]);
+        // the next window starts at the item of slot cb+32
+        if (Bn == cb + kWarp) {
+            i0 += nb + 1;
+            base0 = Bn;
+        } else {
+            i0 += nb;
+            if (nb > 0) base0 = Bl;
         }
-        __syncwarp();
     }
     fold_min(dmin, dm);
 }
@@ -492,8 +531,8 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
 #define TDT_PEEL_MINB 2
 #endif
 __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArgs A) {
-    __shared__ long long s_win[kPeelWarps][kWarp];
     if (!*(volatile int*)&A.ctl->listed) A.lists = nullptr;
+    const bool listed = A.lists != nullptr;
     const int wib = threadIdx.x / kWarp;
     const int64_t gwarp = (int64_t)blockIdx.x * kPeelWarps + wib;
     const int64_t nwarps = (int64_t)gridDim.x * kPeelWarps;
@@ -524,7 +563,8 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
             if (globaltimer_ns() - t_start > kPeelDeadlineNs) set_status(A.ctl, TDT_ERR_TIMEOUT);
         }
         // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
-        process_round(A, r, l, gwarp, nwarps, s_win[wib], &A.ctl->dmin[(ntrans + 1) & 1]);
+        if (listed) process_round<true>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1]);
+        else process_round<false>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1]);
         __syncthreads();
         const uint64_t t_p = globaltimer_ns();
         if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
