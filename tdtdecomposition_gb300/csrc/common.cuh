@@ -122,11 +122,16 @@ __device__ __forceinline__ Off find_sorted(const int32_t* __restrict__ cols, Off
 // ------------------------------------------------------------------ grid barrier
 // Control block shared by the persistent kernels (device memory, zeroed by the
 // host before a launch).
+// The arrival counter and the generation word sit in separate 128-byte lines
+// so the blocks polling the generation do not queue in front of arrivals.
 struct GridCtl {
     unsigned bar_count;
+    unsigned pad0[31];
     unsigned bar_gen;
+    unsigned pad1[31];
     int abort;
     int status;
+    unsigned pad2[30];
 };
 
 // Wait limit of one grid barrier.  A barrier that does not complete within it
@@ -148,16 +153,20 @@ __device__ __forceinline__ bool grid_barrier(GridCtl* ctl, unsigned nblocks) {
             __threadfence();
             atomicAdd(&ctl->bar_gen, 1u);
         } else {
+            // one load per spin; the abort flag and the clock every 32 spins,
+            // and a short sleep once the wait is long
             uint64_t t0 = globaltimer_ns();
             unsigned spins = 0;
             while (ld_acquire_u32(&ctl->bar_gen) == gen) {
-                if (ld_volatile_i32(&ctl->abort)) { ok = 0; break; }
-                if (++spins > 64) __nanosleep(100);
-                if ((spins & 255u) == 0 && globaltimer_ns() - t0 > kBarrierTimeoutNs) {
-                    atomicMax(&ctl->status, (int)TDT_ERR_TIMEOUT);
-                    atomicExch(&ctl->abort, 1);
-                    ok = 0;
-                    break;
+                if ((++spins & 31u) == 0) {
+                    if (ld_volatile_i32(&ctl->abort)) { ok = 0; break; }
+                    if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+                        atomicMax(&ctl->status, (int)TDT_ERR_TIMEOUT);
+                        atomicExch(&ctl->abort, 1);
+                        ok = 0;
+                        break;
+                    }
+                    if (spins > 4096) __nanosleep(200);
                 }
             }
         }

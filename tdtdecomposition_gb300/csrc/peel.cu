@@ -437,16 +437,22 @@ __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, 
     const long long cb0 = gwarp * per_warp;
     const long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
     if (cb0 >= cb1) return;
+    // item of slot cb0 = last i with qb[i] <= cb0: a 32-way search, each step
+    // one load per lane (log32 N dependent loads instead of log2 N)
     long long i0 = 0;
-    if (lane == 0) {
-        long long lo = 0, hi = N - 1;
-        while (lo < hi) {
-            long long mid = (lo + hi + 1) >> 1;
-            if (__ldcg(qb + mid) <= cb0) lo = mid; else hi = mid - 1;
+    {
+        long long lo = 0, hi = N;  // answer in [lo, hi)
+        while (hi - lo > 1) {
+            const long long step = (hi - lo + kWarp - 1) / kWarp;
+            const long long p = lo + (long long)lane * step;
+            const bool le_ = p < hi && __ldcg(qb + p) <= cb0;
+            const unsigned m = __ballot_sync(kFull, le_);
+            const int j = 31 - __clz(m);  // qb[lo] <= cb0 always holds, so m != 0
+            lo += (long long)j * step;
+            hi = lo + step < hi ? lo + step : hi;
         }
         i0 = lo;
     }
-    i0 = __shfl_sync(kFull, i0, 0);
     long long base0 = __ldcg(qb + i0);  // first slot of item i0 (<= cb)
     for (long long cb = cb0; cb < cb1; cb += kWarp) {
         // item i0 holds slot cb; items i0+1.. start at B (strictly increasing,
