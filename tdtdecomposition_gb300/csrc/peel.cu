@@ -56,7 +56,7 @@ struct PeelCtl {
     long long passes;              // level-change passes run (diagnostic)
     int listed;                   // 1: per-edge triangle lists were built (they fit the workspace)
     int list_skip;                // gate of the listing pass and of the list-only setup kernels
-    int enum_skip;                // gate of the in-adjacency build (needed without lists)
+    int enum_skip;                // unused (the in-adjacency is always built)
     int pad0;
     long long rounds;
     long long triangles;
@@ -639,7 +639,7 @@ __global__ void validate_kernel(const int64_t* __restrict__ rp, const int32_t* _
 
 __global__ void indeg_kernel(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t E,
                              int64_t V, int32_t* __restrict__ indeg, const PeelCtl* ctl) {
-    if (*(volatile const int*)&ctl->g.status != 0 || *(volatile const int*)&ctl->enum_skip) return;
+    if (*(volatile const int*)&ctl->g.status != 0) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x)
         atomicAdd(indeg + cols[e], 1);
@@ -648,7 +648,7 @@ __global__ void indeg_kernel(const int32_t* __restrict__ rows, const int32_t* __
 __global__ void csc_fill_kernel(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t E,
                                 int64_t V, const int64_t* __restrict__ cp, int32_t* __restrict__ cursor,
                                 int32_t* __restrict__ in_src, int32_t* __restrict__ in_eid, const PeelCtl* ctl) {
-    if (*(volatile const int*)&ctl->g.status != 0 || *(volatile const int*)&ctl->enum_skip) return;
+    if (*(volatile const int*)&ctl->g.status != 0) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t u = rows[e], v = cols[e];
@@ -697,11 +697,10 @@ __global__ void list_decide_kernel(const int64_t* __restrict__ off, int64_t E, u
     ctl->enum_skip = ok;
 }
 
-// Slot cursors of the listing pass: role A at off[e], role B at off[e] + cA[e],
-// role C at off[e] + cA[e] + cB[e].
-__global__ void list_cursor_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ cA,
-                                   const int32_t* __restrict__ cB, int64_t E, unsigned long long* __restrict__ curA,
-                                   unsigned long long* __restrict__ curB, unsigned long long* __restrict__ curC,
+// Global slot cursors of the listing pass (used by rows listed in place):
+// role A at off[e], role B at off[e] + cA[e].
+__global__ void list_cursor_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ cA, int64_t E,
+                                   unsigned long long* __restrict__ curA, unsigned long long* __restrict__ curB,
                                    const PeelCtl* ctl) {
     if (*(volatile const int*)&ctl->list_skip) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
@@ -709,23 +708,6 @@ __global__ void list_cursor_kernel(const int64_t* __restrict__ off, const int32_
         const unsigned long long o = (unsigned long long)off[e];
         curA[e] = o;
         curB[e] = o + cA[e];
-        curC[e] = o + cA[e] + cB[e];
-    }
-}
-
-// After the listing pass every role-C cursor must sit at the end of its
-// edge's list (and every role-B cursor of rows listed in place at the start
-// of role C); anything else means the two passes disagreed.
-__global__ void list_check_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ cA,
-                                  const int32_t* __restrict__ cB, int64_t E,
-                                  const unsigned long long* __restrict__ curB,
-                                  const unsigned long long* __restrict__ curC, PeelCtl* ctl) {
-    if (*(volatile const int*)&ctl->list_skip) return;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        if (curC[e] != (unsigned long long)off[e + 1]) atomicMax(&ctl->g.status, (int)TDT_ERR_CAPACITY);
-        const unsigned long long b0 = (unsigned long long)off[e] + cA[e];
-        if (curB[e] != b0 && curB[e] != b0 + cB[e]) atomicMax(&ctl->g.status, (int)TDT_ERR_CAPACITY);
     }
 }
 
@@ -823,8 +805,11 @@ int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int
                          int32_t* cC, void* ctl, const int* gate, cudaStream_t st);
 int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* off,
                         const int32_t* cA, const int32_t* cB, unsigned long long* curA_g,
-                        unsigned long long* curB_g, unsigned long long* curC, int2* lists, void* ctl,
-                        const int* gate, int* status, cudaStream_t st);
+                        unsigned long long* curB_g, int2* lists, void* ctl, const int* gate, int* status,
+                        cudaStream_t st);
+int launch_list_transpose(const int64_t* rp, const int64_t* cp, const int32_t* in_eid, int64_t nv, int64_t ne,
+                          const int64_t* off, const int32_t* cA, const int32_t* cB, const int32_t* cC, int2* lists,
+                          int32_t* gcnt, void* ctl, const int* gate, int* status, cudaStream_t st);
 
 namespace {
 struct Carver {
@@ -959,18 +944,16 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     int2* lists = reinterpret_cast<int2*>(reinterpret_cast<char*>(ws) + list_base);
     list_decide_kernel<<<1, 1, 0, st>>>(L.off, E, tail, tail > 0, L.ctl);
     TDT_LAUNCH_CHECK("list_decide");
-    unsigned long long* curC = reinterpret_cast<unsigned long long*>(L.qi[1]);
     unsigned long long* curA = reinterpret_cast<unsigned long long*>(L.qb[0]);
     unsigned long long* curB = reinterpret_cast<unsigned long long*>(L.qb[1]);
-    list_cursor_kernel<<<g_e, tb, 0, st>>>(L.off, cA, cB, E, curA, curB, curC, L.ctl);
+    list_cursor_kernel<<<g_e, tb, 0, st>>>(L.off, cA, E, curA, curB, L.ctl);
     TDT_LAUNCH_CHECK("list_cursor");
-    rc = launch_support_list(rp, cols, V, E, L.off, cA, cB, curA, curB, curC, lists, L.sup_ctl, &L.ctl->list_skip,
+    // roles A and B (the listing pass checks its own counts per row)
+    rc = launch_support_list(rp, cols, V, E, L.off, cA, cB, curA, curB, lists, L.sup_ctl, &L.ctl->list_skip,
                              &L.ctl->g.status, st);
     if (rc) return rc;
-    list_check_kernel<<<g_e, tb, 0, st>>>(L.off, cA, cB, E, curB, curC, L.ctl);
-    TDT_LAUNCH_CHECK("list_check");
-    prof_mark(2, st);
-    // in-adjacency (CSC) of the oriented graph, for the peel without lists
+    // in-adjacency (CSC) of the oriented graph: role-C transpose, and the peel
+    // without lists
     TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
     indeg_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.indeg, L.ctl);
     TDT_LAUNCH_CHECK("indeg");
@@ -979,6 +962,12 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
     csc_fill_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.cp, L.indeg, L.in_src, L.in_eid, L.ctl);
     TDT_LAUNCH_CHECK("csc_fill");
+    // role C of every list, from the role-A lists of each vertex's in-edges
+    rc = launch_list_transpose(rp, L.cp, L.in_eid, V, E, L.off, cA, cB, cC, lists,
+                               reinterpret_cast<int32_t*>(L.qi[1]), L.sup_ctl, &L.ctl->list_skip, &L.ctl->g.status,
+                               st);
+    if (rc) return rc;
+    prof_mark(2, st);
 
     // persistent peel
     int occ = 0;

@@ -31,8 +31,10 @@
 //   kSupList   per-edge triangle lists: the entry of edge e in triangle
 //              (eA, eB, eC) holds the two other edges; e's list occupies
 //              [off[e], off[e+1]) with its role-A entries first, then role B,
-//              then role C.  Slots of roles A and B come from per-row counters
-//              in shared memory, role C from a global cursor.
+//              then role C.  This pass writes roles A and B (slots from the
+//              row's counters in shared memory; both edges are in the source
+//              row, so the stores stay in that row's list region); role C is
+//              filled afterwards from the role-A lists (transpose.cu).
 #include "common.cuh"
 
 namespace tdt {
@@ -105,7 +107,6 @@ struct SupArgs {
     const int32_t* cB_in;           // kSupList: role-B counts (end-of-row check)
     unsigned long long* curA_g;     // kSupList: global cursors for rows searched in place
     unsigned long long* curB_g;
-    unsigned long long* curC;       // kSupList: role-C cursors, start at off + cA + cB
     int2* lists;
     const int* gate;                // non-zero: skip the pass
     int* status;                    // kSupList: set when a row's slots do not end where counted
@@ -187,10 +188,8 @@ __device__ __forceinline__ void on_triangle(const RowState& R, const SupArgs& A,
             sA = atomicAdd(A.curA_g + eA, 1ull);
             sB = atomicAdd(A.curB_g + eB, 1ull);
         }
-        const unsigned long long sC = atomicAdd(A.curC + pos, 1ull);
         A.lists[sA] = make_int2(eB, eC);
         A.lists[sB] = make_int2(eA, eC);
-        A.lists[sC] = make_int2(eA, eB);
     }
 }
 
@@ -596,8 +595,7 @@ int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int
 // Whole-path pass 2: triangle lists (skipped on the device when *gate != 0).
 int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* off,
                         const int32_t* cA, const int32_t* cB, unsigned long long* curA_g, unsigned long long* curB_g,
-                        unsigned long long* curC, int2* lists, void* ctl, const int* gate, int* status,
-                        cudaStream_t st) {
+                        int2* lists, void* ctl, const int* gate, int* status, cudaStream_t st) {
     if (nv <= 0) return TDT_OK;
     OutRows<int64_t> G{rp, 1, cols, nv, ne};
     SupArgs A{};
@@ -606,7 +604,6 @@ int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int6
     A.cB_in = cB;
     A.curA_g = curA_g;
     A.curB_g = curB_g;
-    A.curC = curC;
     A.lists = lists;
     A.gate = gate;
     A.status = status;
