@@ -807,9 +807,9 @@ int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int6
                         const int32_t* cA, const int32_t* cB, unsigned long long* curA_g,
                         unsigned long long* curB_g, int2* lists, void* ctl, const int* gate, int* status,
                         cudaStream_t st);
-int launch_list_transpose(const int64_t* rp, const int64_t* cp, const int32_t* in_eid, int64_t nv, int64_t ne,
-                          const int64_t* off, const int32_t* cA, const int32_t* cB, const int32_t* cC, int2* lists,
-                          int32_t* gcnt, void* ctl, const int* gate, int* status, cudaStream_t st);
+int launch_list_transpose(const int64_t* cp, const int32_t* in_eid, int64_t nv, int64_t ne, const int64_t* off,
+                          const int32_t* cA, const int32_t* cB, int2* lists, unsigned long long* cur, void* next,
+                          const int* gate, int* status, cudaStream_t st);
 
 namespace {
 struct Carver {
@@ -963,9 +963,9 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     csc_fill_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.cp, L.indeg, L.in_src, L.in_eid, L.ctl);
     TDT_LAUNCH_CHECK("csc_fill");
     // role C of every list, from the role-A lists of each vertex's in-edges
-    rc = launch_list_transpose(rp, L.cp, L.in_eid, V, E, L.off, cA, cB, cC, lists,
-                               reinterpret_cast<int32_t*>(L.qi[1]), L.sup_ctl, &L.ctl->list_skip, &L.ctl->g.status,
-                               st);
+    rc = launch_list_transpose(L.cp, L.in_eid, V, E, L.off, cA, cB, lists,
+                               reinterpret_cast<unsigned long long*>(L.qi[1]), L.sup_ctl, &L.ctl->list_skip,
+                               &L.ctl->g.status, st);
     if (rc) return rc;
     prof_mark(2, st);
 
