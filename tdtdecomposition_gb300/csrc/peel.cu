@@ -414,10 +414,72 @@ __device__ bool fixed_start(const PeelArgs& A, int32_t l) {
     return grid_barrier(&A.ctl->g, gridDim.x);
 }
 
+// Item windows: slot cb lies in item i0 (first slot base0); items i0+1.. start
+// at strictly increasing slots, all > cb, so at most 31 start inside
+// (cb, cb+32).  One OR-reduction gives every lane the item of slot cb+lane.
+struct Window {
+    int k;              // this lane's item is i0 + k
+    long long base_l;   // first slot of that item
+    long long i0n;      // item of slot cb+32
+    long long base0n;   // its first slot
+};
+
+__device__ __forceinline__ Window locate(const long long* __restrict__ qb, long long N, long long i0,
+                                         long long base0, long long cb, unsigned le) {
+    const unsigned lane = lane_id();
+    const long long B = (i0 + 1 + lane < N) ? __ldcg(qb + i0 + 1 + lane) : LLONG_MAX;
+    const unsigned bit = (B - cb < kWarp) ? (1u << (unsigned)(B - cb)) : 0u;
+    const unsigned mk = __reduce_or_sync(kFull, bit);
+    Window w;
+    w.k = __popc(mk & le);
+    const long long Bk = __shfl_sync(kFull, B, (w.k + 31) & 31);
+    w.base_l = w.k == 0 ? base0 : Bk;
+    const int nb = __popc(mk);
+    const long long Bn = __shfl_sync(kFull, B, nb);
+    const long long Bl = __shfl_sync(kFull, B, (nb + 31) & 31);
+    if (Bn == cb + kWarp) {
+        w.i0n = i0 + nb + 1;
+        w.base0n = Bn;
+    } else {
+        w.i0n = i0 + nb;
+        w.base0n = nb > 0 ? Bl : base0;
+    }
+    return w;
+}
+
+// The other two edges (f, g) of slot tl of item it; false when the slot is
+// not a triangle (search mode only).
+template <bool Listed>
+__device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, long long tl, int32_t& f, int32_t& g) {
+    if (Listed) {
+        const long long lo = (long long)(unsigned)it.y | ((long long)it.z << 32);
+        const int2 fg = __ldg(A.lists + lo + tl);
+        f = fg.x;
+        g = fg.y;
+        return true;
+    }
+    const int32_t x = it.y, y = it.z, dxo = it.w;
+    int32_t w;
+    if (tl < dxo) {
+        f = (int32_t)(__ldg(A.rp + x) + tl);
+        w = __ldg(A.cols + f);
+    } else {
+        const int64_t kk = __ldg(A.cp + x) + (tl - dxo);
+        w = __ldg(A.in_src + kk);
+        f = __ldg(A.in_eid + kk);
+    }
+    if (w == y) return false;
+    const int64_t gg = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
+                               : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
+    g = (int32_t)gg;
+    return gg >= 0;
+}
+
 // One sub-round: warps gwarp = 0..nwarps-1 share the candidate slots of round r.
 // The smallest decrement result above l is folded into *dmin (the lower bound
-// of the next level).  Compiled once per mode and not inlined, so its
-// registers are allocated apart from the persistent loop around it.
+// of the next level).  Each step covers two 32-slot windows whose loads and
+// decrements are in flight together.  Compiled once per mode and not inlined,
+// so its registers are allocated apart from the persistent loop around it.
 template <bool Listed>
 __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp, long long nwarps,
                                            int* dmin) {
@@ -431,9 +493,8 @@ __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, 
     const long long T = (long long)(packed & kCandMask);
     const long long* __restrict__ qb = A.qb[buf];
     const int4* __restrict__ qi = A.qi[buf];
-    // each warp owns a contiguous range of candidate slots; the item of its
-    // first slot is found once by binary search, later ones step by step
-    const long long per_warp = (((T + nwarps - 1) / nwarps) + 31) & ~31ll;
+    // each warp owns a contiguous range of candidate slots (a multiple of 64)
+    const long long per_warp = (((T + nwarps - 1) / nwarps) + 63) & ~63ll;
     const long long cb0 = gwarp * per_warp;
     const long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
     if (cb0 >= cb1) return;
@@ -453,81 +514,68 @@ __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, 
         }
         i0 = lo;
     }
-    long long base0 = __ldcg(qb + i0);  // first slot of item i0 (<= cb)
-    for (long long cb = cb0; cb < cb1; cb += kWarp) {
-        // item i0 holds slot cb; items i0+1.. start at B (strictly increasing,
-        // all > cb), so the starts inside (cb, cb+32) are at most 31
-        const long long B = (i0 + 1 + lane < N) ? __ldcg(qb + i0 + 1 + lane) : LLONG_MAX;
-        const unsigned bit = (B - cb < kWarp) ? (1u << (unsigned)(B - cb)) : 0u;
-        const unsigned mk = __reduce_or_sync(kFull, bit);
-        const int k = __popc(mk & le);          // this lane's item is i0 + k
-        const long long Bk = __shfl_sync(kFull, B, (k + 31) & 31);
-        const long long base_l = k == 0 ? base0 : Bk;
-        const int nb = __popc(mk);
-        const long long Bn = __shfl_sync(kFull, B, nb);
-        const long long Bl = __shfl_sync(kFull, B, (nb + 31) & 31);
-        const long long t = cb + lane;
-        bool want_f = false, want_g = false;
-        int32_t f = 0, g = 0;
-        if (t < cb1) {
-            const int4 it = __ldcg(qi + i0 + k);
-            const int32_t e = it.x, x = it.y, y = it.z, dxo = it.w;
-            const long long tl = t - base_l;
-            bool tri;
-            if (Listed) {
-                // the slot is one of e's triangles, (f, g) its other edges
-                const long long lo = (long long)(unsigned)x | ((long long)y << 32);
-                const int2 fg = __ldg(A.lists + lo + tl);
-                f = fg.x;
-                g = fg.y;
-                tri = true;
-            } else {
-                int32_t w;
-                if (tl < dxo) {
-                    f = (int32_t)(__ldg(A.rp + x) + tl);
-                    w = __ldg(A.cols + f);
-                } else {
-                    const int64_t kk = __ldg(A.cp + x) + (tl - dxo);
-                    w = __ldg(A.in_src + kk);
-                    f = __ldg(A.in_eid + kk);
-                }
-                tri = w != y;
-                if (tri) {
-                    const int64_t gg = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
-                                               : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
-                    tri = gg >= 0;
-                    g = (int32_t)gg;
-                }
-            }
-            if (tri) {
-                const int32_t rf = __ldcg(&A.es[f].y), rg = __ldcg(&A.es[g].y);
-                const bool af = rf == -1 || rf >= r, ag = rg == -1 || rg >= r;
-                if (af && ag) {
-                    const bool ff = rf == r, fg = rg == r;
-                    // which of f, g this lane decrements (ownership rules above)
-                    const bool df = !ff && (!fg || e < g);
-                    const bool dg = !fg && (!ff || e < f);
-                    // issue both atomics before using either result
-                    int32_t of = 0, og = 0;
-                    if (df) of = atomicSub(&A.es[f].x, 1);
-                    if (dg) og = atomicSub(&A.es[g].x, 1);
-                    want_f = df && of == l + 1;
-                    want_g = dg && og == l + 1;
-                    if (df && of > l + 1) dm = of - 1 < dm ? of - 1 : dm;
-                    if (dg && og > l + 1) dm = og - 1 < dm ? og - 1 : dm;
-                    if (want_f) A.es[f].y = r + 1;
-                    if (want_g) A.es[g].y = r + 1;
-                }
-            }
+    long long base0 = __ldcg(qb + i0);
+    for (long long cb = cb0; cb < cb1; cb += 2 * kWarp) {
+        const Window wa = locate(qb, N, i0, base0, cb, le);
+        const long long cb2 = cb + kWarp;
+        const bool has_b = cb2 < cb1;
+        Window wb;
+        if (has_b) wb = locate(qb, N, wa.i0n, wa.base0n, cb2, le);
+        const long long ta = cb + lane, tb = cb2 + lane;
+        const bool va = ta < cb1, vb = has_b && tb < cb1;
+        int4 ita = make_int4(0, 0, 0, 0), itb = make_int4(0, 0, 0, 0);
+        if (va) ita = __ldcg(qi + i0 + wa.k);
+        if (vb) itb = __ldcg(qi + wa.i0n + wb.k);
+        int32_t fa = 0, ga = 0, fb = 0, gb = 0;
+        bool tra = false, trb = false;
+        if (va) tra = slot_edges<Listed>(A, ita, ta - wa.base_l, fa, ga);
+        if (vb) trb = slot_edges<Listed>(A, itb, tb - wb.base_l, fb, gb);
+        int32_t rfa = -2, rga = -2, rfb = -2, rgb = -2;
+        if (tra) {
+            rfa = __ldcg(&A.es[fa].y);
+            rga = __ldcg(&A.es[ga].y);
         }
-        warp_append2<Listed>(A, nslot, nbuf, want_f, f, want_g, g, l, &A.ctl->fe[nslot]);
-        // the next window starts at the item of slot cb+32
-        if (Bn == cb + kWarp) {
-            i0 += nb + 1;
-            base0 = Bn;
+        if (trb) {
+            rfb = __ldcg(&A.es[fb].y);
+            rgb = __ldcg(&A.es[gb].y);
+        }
+        // a triangle is alive when both other edges are alive or peel in r or r+1;
+        // which of f, g this lane decrements: the ownership rules above
+        bool dfa = false, dga = false, dfb = false, dgb = false;
+        if (tra && (rfa == -1 || rfa >= r) && (rga == -1 || rga >= r)) {
+            const bool ff = rfa == r, fg = rga == r;
+            dfa = !ff && (!fg || ita.x < ga);
+            dga = !fg && (!ff || ita.x < fa);
+        }
+        if (trb && (rfb == -1 || rfb >= r) && (rgb == -1 || rgb >= r)) {
+            const bool ff = rfb == r, fg = rgb == r;
+            dfb = !ff && (!fg || itb.x < gb);
+            dgb = !fg && (!ff || itb.x < fb);
+        }
+        // issue all decrements before using any result
+        int32_t ofa = 0, oga = 0, ofb = 0, ogb = 0;
+        if (dfa) ofa = atomicSub(&A.es[fa].x, 1);
+        if (dga) oga = atomicSub(&A.es[ga].x, 1);
+        if (dfb) ofb = atomicSub(&A.es[fb].x, 1);
+        if (dgb) ogb = atomicSub(&A.es[gb].x, 1);
+        const bool wfa = dfa && ofa == l + 1, wga = dga && oga == l + 1;
+        const bool wfb = dfb && ofb == l + 1, wgb = dgb && ogb == l + 1;
+        if (dfa && ofa > l + 1) dm = ofa - 1 < dm ? ofa - 1 : dm;
+        if (dga && oga > l + 1) dm = oga - 1 < dm ? oga - 1 : dm;
+        if (dfb && ofb > l + 1) dm = ofb - 1 < dm ? ofb - 1 : dm;
+        if (dgb && ogb > l + 1) dm = ogb - 1 < dm ? ogb - 1 : dm;
+        if (wfa) A.es[fa].y = r + 1;
+        if (wga) A.es[ga].y = r + 1;
+        if (wfb) A.es[fb].y = r + 1;
+        if (wgb) A.es[gb].y = r + 1;
+        warp_append2<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, &A.ctl->fe[nslot]);
+        warp_append2<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, &A.ctl->fe[nslot]);
+        if (has_b) {
+            i0 = wb.i0n;
+            base0 = wb.base0n;
         } else {
-            i0 += nb;
-            if (nb > 0) base0 = Bl;
+            i0 = wa.i0n;
+            base0 = wa.base0n;
         }
     }
     fold_min(dmin, dm);
