@@ -140,7 +140,8 @@ class ClockSampler:
 def cpu_sample_scale(args, steps):
     if args.cpu_scale:
         return args.cpu_scale
-    return 17 if steps <= 15 else (16 if steps <= 40 else 15)
+    # about 10 s of CPU work in total on the box's 16 host cores
+    return 18 if steps <= 2 else (17 if steps <= 15 else (16 if steps <= 40 else 15))
 
 
 def cpu_decompose_sample(scale, reps, warm=0):
