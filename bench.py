@@ -10,8 +10,11 @@ outputs) of that graph.
 * e2e:   the same through truss_decompose with host buffers: each step
          copies rows/cols/row_ptr from pinned host memory and reads the
          per-edge truss numbers back;
-* roofline: the dominant kernel's algorithmic bytes (B = 4W + 28E + 4(V+1),
-         W = sum over edges of d+(u)+d+(v)) over its CUDA-event time;
+* roofline: algorithmic bytes over CUDA-event time: a decomposition moves
+         B_dec = 2 B_sup (B_sup = 4W + 28E + 4(V+1), W = sum over edges of
+         d+(u)+d+(v)): the support pass, then one re-enumeration of each
+         edge's triangles (listing + peel); DRAM traffic per decomposition
+         from one ncu capture of this workload sits beside it;
 * cpu_baseline: the oracle port of the reference's CPU flow (OpenMP, all host
          cores) on a bounded R-MAT sample.
 
@@ -336,6 +339,15 @@ def bench_served_small(dev, srv, num_graphs=4096, rate=20000.0):
 
 
 # ---------------------------------------------------------------- GPU arm
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per decomposition
+# of R-MAT scale 22 / edge factor 16, per phase, from one ncu capture of
+# `bench.py --steps 1 --warmup 1 --no-cpu-baseline --no-batched --no-served`
+# (summarised in profiles/launches_rmat_s22_bench.md).
+MEASURED_TRAFFIC = {
+    (22, 16): {"support": 33.02e9, "listing": 152.3e9, "peel": 306.73e9, "outputs": 6.6e9, "setup": 2.4e9},
+}
+
+
 def main_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -450,26 +462,25 @@ def main_ours(args):
     t_sup, t_list, t_peel, t_post = (phases[k] / n for k in range(4))
     # the decomposition's algorithmic bytes B_dec = 2 B_sup: the support pass,
     # then one re-enumeration of each edge's triangles (listing + peel)
-    kernels = {
-        "support_kernel": {"ms": t_sup, "bytes": B_sup, "gbs": B_sup / (t_sup / 1e3) / 1e9},
-        "peel_phase": {"ms": t_list + t_peel, "bytes": B_sup, "gbs": B_sup / ((t_list + t_peel) / 1e3) / 1e9},
+    mt = MEASURED_TRAFFIC.get((scale, ef))
+    B_dec = 2 * B_sup
+    ach = B_dec / (ms_step / 1e3) / 1e9
+    phases_ms = {"support": t_sup, "listing": t_list, "peel": t_peel, "outputs": t_post}
+    per_kernel = {
+        "support_kernel": {"ms": round(t_sup, 4), "algorithmic_bytes": B_sup,
+                           "achieved_gbs": round(B_sup / (t_sup / 1e3) / 1e9, 1),
+                           "traffic": mt["support"] if mt else None},
+        "reenumeration (listing + transpose + peel kernels)": {
+            "ms": round(t_list + t_peel, 4), "algorithmic_bytes": B_sup,
+            "achieved_gbs": round(B_sup / ((t_list + t_peel) / 1e3) / 1e9, 1),
+            "traffic": (mt["listing"] + mt["peel"]) if mt else None},
+        "peel_kernel": {"ms": round(t_peel, 4), "traffic": mt["peel"] if mt else None,
+                        "dram_gbs": round(mt["peel"] / (t_peel / 1e3) / 1e9, 1) if mt else None},
     }
-    dom = max(kernels, key=lambda k: kernels[k]["ms"])
-    traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "traffic_rmat.json")
-    if os.path.exists(tr_path):
-        try:
-            tj = json.load(open(tr_path))
-            traffic = tj.get(dom, {}).get("bytes_per_launch_full")
-        except Exception:
-            traffic = None
-    ach = kernels[dom]["gbs"]
-    roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-            "traffic": traffic, "peak_source": peak_src,
-            "per_kernel": {k: {"ms": round(v["ms"], 4), "achieved_gbs": round(v["gbs"], 1),
-                               "algorithmic_bytes": v["bytes"]} for k, v in kernels.items()},
-            "phase_ms": {"support": t_sup, "listing": t_list, "peel": t_peel, "outputs": t_post},
-            "decomposition_gbs_of_2Bsup": 2 * B_sup / (ms_step / 1e3) / 1e9}
+    roof = {"bound": "hbm", "kernel": "decomposition (all kernels of one step)", "achieved": ach, "peak": peak,
+            "unit": "GB/s", "frac": ach / peak, "traffic": sum(mt.values()) if mt else None,
+            "algorithmic_bytes": B_dec, "peak_source": peak_src, "per_kernel": per_kernel, "phase_ms": phases_ms,
+            "traffic_source": "ncu capture of this workload (profiles/launches_rmat_s22_bench.md)" if mt else None}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
