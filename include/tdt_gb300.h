@@ -68,6 +68,17 @@ int tdt_profile_stop(float *ms_phase, int *ncalls);
  * defaults.  Affects calls launched afterwards from any thread. */
 void tdt_set_support_caps(int warp_cap, int heavy_cap);
 
+/* Testing knobs of the failure paths (no counterpart in the reference, which
+ * has no bounded waits).  tdt_set_peel_deadline_ns: wall-clock budget of the
+ * peel launches that follow (<= 0 restores the default of 120 s); a run past
+ * it stops between sub-rounds with TDT_ERR_TIMEOUT in its stats.
+ * tdt_test_barrier_timeout: launches 8 blocks at a grid barrier that one of
+ * them never reaches; the others give up after limit_ns (1 ms .. 2 s) and the
+ * call returns the device status, TDT_ERR_TIMEOUT.  workspace: >= 4096 bytes
+ * of device memory.  Blocks the calling thread until the kernel ends. */
+void tdt_set_peel_deadline_ns(long long ns);
+int tdt_test_barrier_timeout(void *workspace, long long limit_ns, cudaStream_t stream);
+
 /* =====================================================================
  * Drop-in `trusstensor` operators.
  * Each replaces the pybind op of the same name in

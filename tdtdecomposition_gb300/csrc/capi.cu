@@ -88,6 +88,8 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
              uint8_t* in_k, int32_t* support_out, int64_t* stats, void* ws, size_t ws_bytes, cudaStream_t st);
 
 void set_support_caps(int warp_cap, int heavy_cap);
+void set_peel_deadline(long long ns);
+int test_barrier_timeout(void* ws, long long limit_ns, cudaStream_t st);
 int launch_support_accum_i32(const int32_t* rp, int32_t stride, const int32_t* cols, int64_t nv, int64_t ne,
                              int32_t* out, cudaStream_t st);
 
@@ -127,6 +129,10 @@ API const char* tdt_last_error(void) { return g_err; }
 API unsigned long long tdt_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
 API void tdt_set_support_caps(int warp_cap, int heavy_cap) { set_support_caps(warp_cap, heavy_cap); }
+API void tdt_set_peel_deadline_ns(long long ns) { set_peel_deadline(ns); }
+API int tdt_test_barrier_timeout(void* workspace, long long limit_ns, cudaStream_t stream) {
+    return test_barrier_timeout(workspace, limit_ns, stream);
+}
 
 API int tdt_profile_start(int max_calls) {
     TDT_CHECK_ARG(max_calls > 0 && max_calls <= 4096, "max_calls out of range");

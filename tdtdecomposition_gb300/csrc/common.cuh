@@ -140,7 +140,8 @@ constexpr uint64_t kBarrierTimeoutNs = 20ull * 1000ull * 1000ull * 1000ull;
 
 // Sense-free generation barrier over all blocks of a cooperative launch.
 // Returns false when the run is being aborted (timeout or an error elsewhere).
-__device__ __forceinline__ bool grid_barrier(GridCtl* ctl, unsigned nblocks) {
+__device__ __forceinline__ bool grid_barrier(GridCtl* ctl, unsigned nblocks,
+                                             uint64_t limit_ns = kBarrierTimeoutNs) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -160,7 +161,7 @@ __device__ __forceinline__ bool grid_barrier(GridCtl* ctl, unsigned nblocks) {
             while (ld_acquire_u32(&ctl->bar_gen) == gen) {
                 if ((++spins & 31u) == 0) {
                     if (ld_volatile_i32(&ctl->abort)) { ok = 0; break; }
-                    if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+                    if (globaltimer_ns() - t0 > limit_ns) {
                         atomicMax(&ctl->status, (int)TDT_ERR_TIMEOUT);
                         atomicExch(&ctl->abort, 1);
                         ok = 0;

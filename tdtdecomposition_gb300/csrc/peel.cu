@@ -83,6 +83,7 @@ struct PeelArgs {
     int64_t V, E, round_cap;
     int32_t mode;         // 0: full decomposition, 1: fixed-level peel (k-truss search)
     int32_t fixed_level;
+    unsigned long long deadline_ns;  // wall-clock budget of the launch
     PeelCtl* ctl;
 };
 
@@ -614,7 +615,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
             A.round_level[r] = l;
             A.ctl->q[(r + 2) % 3] = 0;
             A.ctl->fe[(r + 2) % 3] = 0;
-            if (globaltimer_ns() - t_start > kPeelDeadlineNs) set_status(A.ctl, TDT_ERR_TIMEOUT);
+            if (globaltimer_ns() - t_start > A.deadline_ns) set_status(A.ctl, TDT_ERR_TIMEOUT);
         }
         // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
         if (listed) process_round<true>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1]);
@@ -849,6 +850,31 @@ __global__ void stats_final_kernel(PeelCtl* ctl, int64_t* stats, int mode) {
 // ------------------------------------------------------------------ host side
 void prof_mark(int phase, cudaStream_t st);
 
+// Test hook: wall-clock budget of the next peel launches (<= 0: the default).
+static long long g_peel_deadline_ns = 0;
+void set_peel_deadline(long long ns) { g_peel_deadline_ns = ns; }
+
+// A grid barrier that one block never reaches: the others wait limit_ns, then
+// leave with TDT_ERR_TIMEOUT in ctl->status (the test of the bounded waits).
+__global__ void barrier_probe_kernel(GridCtl* ctl, unsigned long long limit_ns) {
+    if (blockIdx.x == 0) return;
+    grid_barrier(ctl, gridDim.x, limit_ns);
+}
+
+int test_barrier_timeout(void* ws, long long limit_ns, cudaStream_t st) {
+    TDT_CHECK_ARG(ws != nullptr, "null workspace");
+    TDT_CHECK_ARG(limit_ns >= 1000000ll && limit_ns <= 2000000000ll, "limit %lld ns outside [1 ms, 2 s]",
+                  limit_ns);
+    GridCtl* ctl = reinterpret_cast<GridCtl*>(ws);
+    TDT_CUDA(cudaMemsetAsync(ctl, 0, sizeof(GridCtl), st));
+    barrier_probe_kernel<<<8, 32, 0, st>>>(ctl, (unsigned long long)limit_ns);
+    TDT_LAUNCH_CHECK("barrier_probe");
+    int status = 0;
+    TDT_CUDA(cudaMemcpyAsync(&status, &ctl->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TDT_CUDA(cudaStreamSynchronize(st));
+    return status;
+}
+
 int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* cA, int32_t* cB,
                          int32_t* cC, void* ctl, const int* gate, cudaStream_t st);
 int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* off,
@@ -1033,6 +1059,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     A.V = V; A.E = E; A.round_cap = E + 2;
     A.mode = mode == 0 ? 0 : 1;
     A.fixed_level = fixed_level;
+    A.deadline_ns = g_peel_deadline_ns > 0 ? (unsigned long long)g_peel_deadline_ns : kPeelDeadlineNs;
     A.ctl = L.ctl;
     if (di.sms * occ > 4096) occ = 4096 / di.sms;
     dim3 grid(di.sms * occ), block(kPeelBlock);
