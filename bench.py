@@ -221,6 +221,21 @@ def bench_batched(dev, steps, warmup, num_graphs=4096):
     b.record(stream)
     torch.cuda.synchronize()
     ms_batched = a.elapsed_time(b) / steps
+    # the same run recorded once as a CUDA graph and replayed
+    cap = B.capture(bt, workspace=T.Workspace(dev), lists=tuned[2])
+    for _ in range(warmup):
+        cap.replay(sync=False)
+    torch.cuda.synchronize()
+    rep = cap.replay()
+    if not torch.equal(rep.truss, ref.truss):
+        raise SystemExit("CUDA-graph replay differs from the eager batched run")
+    a.record(stream)
+    for _ in range(steps):
+        cap.replay(sync=False)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms_graph = a.elapsed_time(b) / steps
+    del cap
     autotune.reset()
     # plain path: the same graphs, one call (and one result read-back) per graph
     eoh, voh = eo.cpu().tolist(), vo.cpu().tolist()
@@ -245,6 +260,8 @@ def bench_batched(dev, steps, warmup, num_graphs=4096):
             "value": E / (ms_batched / 1e3), "unit": UNIT, "ms_per_step": ms_batched,
             "plain_value": E / s_plain, "plain_s": s_plain, "speedup_vs_plain": (E / (ms_batched / 1e3)) / (E / s_plain),
             "kmax_max": int(ref.kmax.max()), "sub_rounds": ref.union.rounds,
+            "cuda_graph": {"ms_per_step": ms_graph, "value": E / (ms_graph / 1e3),
+                           "note": "support, listing, the cooperative peel and outputs captured once, replayed"},
             "autotuned": {"warp_cap": tuned[0], "heavy_cap": tuned[1], "lists": tuned[2]},
             "host_generation_s": t_gen, "results_identical_to_plain": True}
 

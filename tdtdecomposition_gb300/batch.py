@@ -86,3 +86,71 @@ def per_graph(batch: GraphBatch, result: BatchResult, g: int):
     """Truss numbers of graph g (its own CSR edge order)."""
     a, b = int(batch.edge_offsets[g]), int(batch.edge_offsets[g + 1])
     return result.truss[a:b]
+
+
+class CapturedBatch:
+    """One batched decomposition recorded as a CUDA graph and replayed.
+
+    Everything a replay touches is allocated at capture: the outputs, the
+    workspace (base part plus a fixed triangle-list tail; the device decides
+    per replay whether the lists fit) and the per-graph segment ids.  A replay
+    re-reads the batch's CSR tensors in place, so new graphs of the same
+    shape can be copied into them between replays.  replay() returns the
+    per-graph results after checking the run's device status."""
+
+    def __init__(self, batch: GraphBatch, workspace=None, lists="auto", list_budget=None, stream=None):
+        from . import _lib
+        L = _lib.load()
+        g = batch.graph
+        rows, cols, rp = T._graph_arrays(g)
+        dev = cols.device
+        self.batch = batch
+        V, E = rp.shape[0] - 1, cols.shape[0]
+        self.truss = torch.empty(E, dtype=torch.int32, device=dev)
+        self.e_truss = torch.empty(max(E, 1), dtype=torch.int32, device=dev)
+        self.cap = E + 2
+        self.ptr = torch.empty(self.cap, dtype=torch.int32, device=dev)
+        self.stats = torch.zeros(T.STAT_COUNT, dtype=torch.int64, device=dev)
+        wso = T._ws_for(dev, workspace)
+        base = (L.tdt_decompose_workspace_bytes(V, E) + 255) // 256 * 256
+        tail = int(list_budget) if list_budget is not None else T._list_bytes(wso, cols, rp, lists, base)
+        self.ws = wso.get(base + tail)
+        eo = batch.edge_offsets.to(dev)
+        G = batch.num_graphs
+        self.seg = torch.repeat_interleave(torch.arange(G, device=dev), eo[1:] - eo[:-1])
+        self.kmax = torch.full((G,), 2, dtype=torch.int64, device=dev)
+        self.stream = stream or torch.cuda.Stream(dev)
+        args = (rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
+                self.truss.data_ptr(), self.e_truss.data_ptr(), self.ptr.data_ptr(), self.cap,
+                self.stats.data_ptr(), self.ws.data_ptr(), self.ws.numel())
+
+        def body():
+            s = torch.cuda.current_stream(dev).cuda_stream
+            _lib.check(L.tdt_truss_decompose(*args, s), "tdt_truss_decompose")
+            self.kmax.fill_(2)
+            self.kmax.scatter_reduce_(0, self.seg, self.truss.to(torch.int64), reduce="amax", include_self=True)
+
+        # one eager run on the capture stream (kernel attributes, caches), then capture
+        self.stream.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(self.stream):
+            body()
+        self.stream.synchronize()
+        T._check_stats(self.stats.cpu(), "tdt_truss_decompose")
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, stream=self.stream, capture_error_mode="relaxed"):
+            body()
+
+    def replay(self, sync=True):
+        self.graph.replay()
+        if not sync:
+            return None
+        sh = self.stats.cpu()
+        T._check_stats(sh, "tdt_truss_decompose (graph replay)")
+        union = T.TrussResult(self.truss, self.e_truss[: int(sh[T.STAT_NETRUSS])], self.ptr[: int(sh[T.STAT_NPTR])],
+                              int(sh[T.STAT_KMAX]), int(sh[T.STAT_TRIANGLES]), int(sh[T.STAT_ROUNDS]))
+        return BatchResult(self.truss, self.kmax, union)
+
+
+def capture(batch: GraphBatch, workspace=None, lists="auto", list_budget=None):
+    """CUDA-graph capture of decompose(batch) (see CapturedBatch)."""
+    return CapturedBatch(batch, workspace=workspace, lists=lists, list_budget=list_budget)

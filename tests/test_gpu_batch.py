@@ -76,3 +76,30 @@ def test_autotune_picks_a_split_and_keeps_results():
         assert torch.equal(got.truss, ref.truss) and torch.equal(got.e_truss, ref.e_truss)
     finally:
         autotune.reset()
+
+
+@pytest.mark.parametrize("list_budget", [None, 0])
+def test_captured_batch_replays_equal_the_eager_run(list_budget):
+    """A batch recorded once as a CUDA graph (support, listing, the persistent
+    cooperative peel and the outputs) and replayed: every replay gives the
+    eager run's truss numbers, per-graph kmax and e_truss order; new graphs of
+    the same shape copied into the inputs are decomposed by the next replay.
+    list_budget 0 captures the search peel (no list tail)."""
+    graphs = _small_batch(num=40, seed=11)
+    bt = B.pack_host(graphs)
+    eager = B.decompose(bt)
+    cap = B.capture(bt, list_budget=list_budget)
+    for _ in range(2):
+        r = cap.replay()
+        assert torch.equal(r.truss, eager.truss)
+        assert torch.equal(r.kmax, eager.kmax)
+        assert torch.equal(r.union.e_truss, eager.union.e_truss)
+        assert torch.equal(r.union.ptr_truss, eager.union.ptr_truss)
+    # replays re-read the inputs: an invalid CSR copied in is reported by the
+    # next replay, and the restored one decomposes again
+    saved = bt.graph.columns.clone()
+    bt.graph.columns.copy_(bt.graph.rows)
+    with pytest.raises(T._lib.TdtError):
+        cap.replay()
+    bt.graph.columns.copy_(saved)
+    assert torch.equal(cap.replay().truss, eager.truss)
