@@ -225,6 +225,7 @@ enum tdt_stat_index {
     TDT_STAT_TRIANGLES = 4,  /* triangle count                                 */
     TDT_STAT_NETRUSS = 5,    /* entries written to e_truss                     */
     TDT_STAT_ALIVE = 6,      /* k-truss search: edges left in the k-truss      */
+    TDT_STAT_LISTED = 7,     /* 1: the peel read per-edge triangle lists; 0: it searched */
     TDT_STAT_COUNT = 8
 };
 

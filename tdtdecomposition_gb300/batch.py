@@ -115,6 +115,7 @@ class CapturedBatch:
         base = (L.tdt_decompose_workspace_bytes(V, E) + 255) // 256 * 256
         tail = int(list_budget) if list_budget is not None else T._list_bytes(wso, cols, rp, lists, base)
         self.ws = wso.get(base + tail)
+        self.ws_bytes = base + tail
         eo = batch.edge_offsets.to(dev)
         G = batch.num_graphs
         self.seg = torch.repeat_interleave(torch.arange(G, device=dev), eo[1:] - eo[:-1])
@@ -122,7 +123,7 @@ class CapturedBatch:
         self.stream = stream or torch.cuda.Stream(dev)
         args = (rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
                 self.truss.data_ptr(), self.e_truss.data_ptr(), self.ptr.data_ptr(), self.cap,
-                self.stats.data_ptr(), self.ws.data_ptr(), self.ws.numel())
+                self.stats.data_ptr(), self.ws.data_ptr(), self.ws_bytes)
 
         def body():
             s = torch.cuda.current_stream(dev).cuda_stream
@@ -147,7 +148,8 @@ class CapturedBatch:
         sh = self.stats.cpu()
         T._check_stats(sh, "tdt_truss_decompose (graph replay)")
         union = T.TrussResult(self.truss, self.e_truss[: int(sh[T.STAT_NETRUSS])], self.ptr[: int(sh[T.STAT_NPTR])],
-                              int(sh[T.STAT_KMAX]), int(sh[T.STAT_TRIANGLES]), int(sh[T.STAT_ROUNDS]))
+                              int(sh[T.STAT_KMAX]), int(sh[T.STAT_TRIANGLES]), int(sh[T.STAT_ROUNDS]),
+                              bool(sh[T.STAT_LISTED]))
         return BatchResult(self.truss, self.kmax, union)
 
 

@@ -840,6 +840,7 @@ __global__ void ktruss_out_kernel(const int2* __restrict__ es, int64_t E, uint8_
 
 __global__ void stats_final_kernel(PeelCtl* ctl, int64_t* stats, int mode) {
     stats[TDT_STAT_STATUS] = ctl->g.status;
+    stats[TDT_STAT_LISTED] = ctl->listed;
     if (mode != 0) {
         stats[TDT_STAT_ALIVE] = (long long)ctl->alive;
         stats[TDT_STAT_ROUNDS] = ctl->rounds;

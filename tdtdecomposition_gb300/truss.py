@@ -13,7 +13,7 @@ import torch
 
 from . import _lib
 
-STAT_STATUS, STAT_KMAX, STAT_NPTR, STAT_ROUNDS, STAT_TRIANGLES, STAT_NETRUSS, STAT_ALIVE = range(7)
+STAT_STATUS, STAT_KMAX, STAT_NPTR, STAT_ROUNDS, STAT_TRIANGLES, STAT_NETRUSS, STAT_ALIVE, STAT_LISTED = range(8)
 STAT_COUNT = 8
 
 
@@ -24,6 +24,7 @@ class TrussResult(NamedTuple):
     kmax: int
     triangles: int
     rounds: int
+    listed: bool = False      # the peel read per-edge triangle lists (else it searched)
 
 
 class Workspace:
@@ -129,16 +130,18 @@ def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto",
     tail = int(list_budget) if list_budget is not None else _list_bytes(wso, cols, rp, lists, base)
     ws = wso.get(base + tail)
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
+    # pass the requested size, not the (possibly larger, shared) buffer: the
+    # device keeps lists exactly when the tail it is given holds them
     rc = L.tdt_truss_decompose(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
                                truss.data_ptr(), e_truss.data_ptr(), ptr.data_ptr(), cap, stats.data_ptr(),
-                               ws.data_ptr(), ws.numel(), s)
+                               ws.data_ptr(), base + tail, s)
     _lib.check(rc, "tdt_truss_decompose")
     if not sync:
         return truss, e_truss, ptr, stats
     sh = stats.cpu()
     _check_stats(sh, "tdt_truss_decompose")
     return TrussResult(truss, e_truss[: int(sh[STAT_NETRUSS])], ptr[: int(sh[STAT_NPTR])], int(sh[STAT_KMAX]),
-                       int(sh[STAT_TRIANGLES]), int(sh[STAT_ROUNDS]))
+                       int(sh[STAT_TRIANGLES]), int(sh[STAT_ROUNDS]), bool(sh[STAT_LISTED]))
 
 
 def ktruss_search(graph, k, workspace=None, stream=None, lists="auto"):
@@ -152,10 +155,11 @@ def ktruss_search(graph, k, workspace=None, stream=None, lists="auto"):
     stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
     wso = _ws_for(dev, workspace)
     base = (L.tdt_decompose_workspace_bytes(V, E) + 255) // 256 * 256
-    ws = wso.get(base + _list_bytes(wso, cols, rp, lists, base))
+    tail = _list_bytes(wso, cols, rp, lists, base)
+    ws = wso.get(base + tail)
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
     rc = L.tdt_ktruss_search(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
-                             int(k), mask.data_ptr(), stats.data_ptr(), ws.data_ptr(), ws.numel(), s)
+                             int(k), mask.data_ptr(), stats.data_ptr(), ws.data_ptr(), base + tail, s)
     _lib.check(rc, "tdt_ktruss_search")
     _check_stats(stats.cpu(), "tdt_ktruss_search")
     return mask

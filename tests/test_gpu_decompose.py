@@ -26,6 +26,7 @@ def test_decompose_matches_reference_peel_order(name, lists):
     d = GD.load(name)
     g = graph_of(d["ref_rows"], d["ref_cols"], d["ref_rp"])
     res = T.truss_decompose(g, lists=lists)
+    assert res.listed == (lists and int(d["ref_support"].sum()) > 0)
     assert res.kmax == int(d["sg_kmax2"]) == int(d["sg_kmax1"])
     assert np.array_equal(res.e_truss.cpu().numpy(), d["sg_e_truss2"])
     assert np.array_equal(res.e_truss.cpu().numpy(), d["sg_e_truss1"])
