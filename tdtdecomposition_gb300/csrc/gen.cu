@@ -38,6 +38,27 @@ __global__ void rmat_kernel(int scale, int64_t m, uint64_t key, uint64_t ta, uin
     }
 }
 
+// Chung-Lu: draw i takes stream values 2i and 2i+1 modulo the total integer
+// weight and maps each to the first vertex whose cumulative weight exceeds it
+// (cum: inclusive prefix sums of the per-vertex integer weights, n entries).
+__global__ void chung_lu_kernel(int64_t n, int64_t m, uint64_t key, const uint64_t* __restrict__ cum,
+                                uint64_t total, int32_t* __restrict__ src, int32_t* __restrict__ dst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t out[2];
+        for (int k = 0; k < 2; k++) {
+            const uint64_t r = splitmix64(key + 2ull * (uint64_t)i + (uint64_t)k) % total;
+            int64_t lo = 0, hi = n;  // first index with cum > r
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (__ldg(cum + mid) > r) hi = mid; else lo = mid + 1;
+            }
+            out[k] = (int32_t)(lo < n ? lo : n - 1);
+        }
+        src[i] = out[0];
+        dst[i] = out[1];
+    }
+}
+
 }  // namespace tdt
 
 using namespace tdt;
@@ -58,6 +79,24 @@ API int tdt_gen_rmat(int32_t scale, int64_t m, uint64_t seed, uint64_t ta, uint6
     rmat_kernel<<<grid_for(m, 256, di.sms, 16), 256, 0, (cudaStream_t)stream>>>(scale, m, splitmix64(seed), ta, tab,
                                                                              tabc, src, dst);
     TDT_LAUNCH_CHECK("rmat");
+    return TDT_OK;
+}
+
+// Chung-Lu edge list on the device (src/dst int32[m]) from the cumulative
+// integer weights cum (device, uint64[n], strictly positive weights).
+API int tdt_gen_chung_lu(int64_t n, int64_t m, uint64_t seed, const uint64_t* cum, uint64_t total, int32_t* src,
+                         int32_t* dst, tdt_stream_t stream) {
+    TDT_CHECK_ARG(n >= 1 && n <= (int64_t)INT32_MAX, "n %lld out of range", (long long)n);
+    TDT_CHECK_ARG(m >= 0, "negative edge count");
+    TDT_CHECK_ARG(total >= 1, "total weight must be positive");
+    if (m == 0) return TDT_OK;
+    TDT_CHECK_ARG(src && dst && cum, "null pointer");
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    chung_lu_kernel<<<grid_for(m, 256, di.sms, 16), 256, 0, (cudaStream_t)stream>>>(n, m, splitmix64(seed), cum,
+                                                                                 total, src, dst);
+    TDT_LAUNCH_CHECK("chung_lu");
     return TDT_OK;
 }
 

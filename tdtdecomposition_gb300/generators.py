@@ -93,10 +93,8 @@ def rmat_edges_device(scale, m, a=0.57, b=0.19, c=0.19, seed=1, device="cuda"):
     return src, dst
 
 
-def chung_lu_edges(n, gamma=2.1, mean_degree=40.0, max_degree=1 << 20, seed=2, m=None):
-    """Chung-Lu: expected degree w_i = c * (i+1)^(-1/(gamma-1)), capped at
-    max_degree, scaled to the mean degree; m = n*mean/2 draws, each endpoint
-    drawn with probability proportional to w (integer inverse CDF)."""
+def chung_lu_weights(n, gamma=2.1, mean_degree=40.0, max_degree=1 << 20):
+    """Cumulative integer weights (uint64[n]) of chung_lu_edges."""
     i = np.arange(n, dtype=np.float64)
     w = (i + 1.0) ** (-1.0 / (gamma - 1.0))
     w *= mean_degree * n / w.sum()
@@ -104,13 +102,44 @@ def chung_lu_edges(n, gamma=2.1, mean_degree=40.0, max_degree=1 << 20, seed=2, m
     w *= mean_degree * n / w.sum()
     w = np.minimum(w, float(max_degree))
     wi = np.maximum(np.round(w * 1024.0), 1).astype(np.uint64)
-    cum = np.cumsum(wi)
+    return np.cumsum(wi)
+
+
+def chung_lu_edges(n, gamma=2.1, mean_degree=40.0, max_degree=1 << 20, seed=2, m=None):
+    """Chung-Lu: expected degree w_i = c * (i+1)^(-1/(gamma-1)), capped at
+    max_degree, scaled to the mean degree; m = n*mean/2 draws, each endpoint
+    drawn with probability proportional to w (integer inverse CDF over
+    chung_lu_weights)."""
+    cum = chung_lu_weights(n, gamma, mean_degree, max_degree)
     total = int(cum[-1])
     if m is None:
         m = int(n * mean_degree / 2)
     r = stream(seed, 0, 2 * m).reshape(m, 2) % _U(total)
     src = np.searchsorted(cum, r[:, 0], side="right").astype(np.int32)
     dst = np.searchsorted(cum, r[:, 1], side="right").astype(np.int32)
+    return src, dst
+
+
+def chung_lu_edges_device(n, gamma=2.1, mean_degree=40.0, max_degree=1 << 20, seed=2, m=None, device="cuda"):
+    """chung_lu_edges on the GPU (tdt_gen_chung_lu): the same edges, as int32
+    CUDA tensors."""
+    import torch
+    from . import _lib
+    L = _lib.load()
+    cum = chung_lu_weights(n, gamma, mean_degree, max_degree)
+    total = int(cum[-1])
+    if m is None:
+        m = int(n * mean_degree / 2)
+    cum_d = torch.from_numpy(cum.view(np.int64)).to(device)
+    src = torch.empty(m, dtype=torch.int32, device=device)
+    dst = torch.empty(m, dtype=torch.int32, device=device)
+    fn = L.tdt_gen_chung_lu
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    _lib.check(fn(n, m, seed, cum_d.data_ptr(), total, src.data_ptr(), dst.data_ptr(),
+                  torch.cuda.current_stream().cuda_stream), "tdt_gen_chung_lu")
+    del cum_d
     return src, dst
 
 
