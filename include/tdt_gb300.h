@@ -77,6 +77,13 @@ void tdt_set_support_caps(int warp_cap, int heavy_cap);
  * call returns the device status, TDT_ERR_TIMEOUT.  workspace: >= 4096 bytes
  * of device memory.  Blocks the calling thread until the kernel ends. */
 void tdt_set_peel_deadline_ns(long long ns);
+
+/* Testing knob of tdt_ktruss_search: the low-support edges that start the
+ * peel are queued in batches of at most `items` edges and `cands` candidate
+ * slots per sub-round (defaults 2^27 and 2^35, for graphs whose low-support
+ * edges outnumber the queue); lower values let small graphs run several
+ * batches.  <= 0 restores a default.  Results do not depend on it. */
+void tdt_set_ktruss_batch_caps(long long items, long long cands);
 int tdt_test_barrier_timeout(void *workspace, long long limit_ns, cudaStream_t stream);
 
 /* =====================================================================

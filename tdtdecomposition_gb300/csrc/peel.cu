@@ -84,6 +84,7 @@ struct PeelArgs {
     int32_t mode;         // 0: full decomposition, 1: fixed-level peel (k-truss search)
     int32_t fixed_level;
     unsigned long long deadline_ns;  // wall-clock budget of the launch
+    unsigned long long fixed_item_cap, fixed_cand_cap;  // k-truss collection batch limits
     PeelCtl* ctl;
 };
 
@@ -397,22 +398,82 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
     return grid_barrier(&A.ctl->g, gridDim.x);
 }
 
-// Fixed-level start (k-truss search): F_0 = edges with support <= l.
-__device__ bool fixed_start(const PeelArgs& A, int32_t l) {
+// k-truss search (fixed level l): the frontier is every alive edge with
+// support <= l, collected in batches.  A collection pass queues such edges
+// while the round's queue stays under fixed_item_cap items and fixed_cand_cap
+// candidate slots (by default far below the packed counter's limits, which
+// leaves room for warps that read the count before others added to it);
+// edges left out stay alive and are taken by the next pass, which runs
+// whenever a sub-round queues nothing.  The k-truss does not depend on how the
+// peel is split into rounds, so the batches change no result; they keep the
+// rounds of graphs whose low-support edges outnumber the queue within it.
+constexpr unsigned long long kFixedItemCap = 1ull << 27;
+constexpr unsigned long long kFixedCandCap = 1ull << 35;
+
+__device__ __forceinline__ void warp_append_capped(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
+                                                   int32_t s, int r_next, unsigned long long* nfront) {
+    const unsigned lane = lane_id();
+    if (__ballot_sync(kFull, want) == 0) return;
+    int4 it;
+    long long dx;
+    const bool q = A.lists ? make_item<true>(A, want, s, e, it, dx) : make_item<false>(A, want, s, e, it, dx);
+    const unsigned m = __ballot_sync(kFull, q);
+    const long long c = q ? dx : 0;
+    const long long incl = warp_incl_scan(c);
+    const long long tot = __shfl_sync(kFull, incl, 31);
+    const int n = __popc(m);
+    int ok = 1;
+    unsigned long long old = 0;
+    if (lane == 0 && n > 0) {
+        const unsigned long long cur = ld_cg_u64(&A.ctl->q[slot]);
+        // a batch always takes something (an empty queue accepts any warp)
+        if (cur != 0 && ((cur >> kCandBits) + (unsigned long long)n > A.fixed_item_cap ||
+                         (cur & kCandMask) + (unsigned long long)tot > A.fixed_cand_cap)) {
+            ok = 0;
+        } else {
+            old = atomicAdd(&A.ctl->q[slot], ((unsigned long long)n << kCandBits) + (unsigned long long)tot);
+            const unsigned long long it0 = old >> kCandBits, c0 = old & kCandMask;
+            if (it0 + n >= (1ull << kItemBits) || c0 + tot >= (1ull << kCandBits) || (long long)(it0 + n) > A.E)
+                set_status(A.ctl, TDT_ERR_CAPACITY);
+        }
+    }
+    ok = __shfl_sync(kFull, ok, 0);
+    old = __shfl_sync(kFull, old, 0);
+    // edges without candidates use no queue space and are always taken
+    const bool acc = want && (!q || ok);
+    if (acc) A.es[e].y = r_next;
+    const unsigned ma = __ballot_sync(kFull, acc);
+    if (lane == 0 && ma) atomicAdd(nfront, (unsigned long long)__popc(ma));
+    if (q && ok) {
+        const long long idx = (long long)(old >> kCandBits) + __popc(m & lanemask_lt());
+        if (idx < A.E) {
+            A.qi[buf][idx] = it;
+            A.qb[buf][idx] = (long long)(old & kCandMask) + incl - c;
+        }
+    }
+}
+
+// One collection pass for sub-round r_next; true when it took an edge.
+__device__ bool fixed_collect(const PeelArgs& A, int32_t l, int r_next, int& np) {
     const unsigned lane = lane_id();
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    const int slot = r_next % 3, buf = r_next & 1;
+    pass_start(A, np);
     for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; base < A.E;
          base += nthreads) {
         const int64_t e = base + lane;
         bool want = false;
         int32_t s = 0;
         if (e < A.E) {
-            s = __ldcg(&A.es[e].x);
-            if (s <= l) { want = true; A.es[e].y = 0; }
+            const int2 st = __ldcg(A.es + e);
+            s = st.x;
+            want = st.y == -1 && s <= l;
         }
-        warp_append(A, 0, 0, want, (int32_t)e, s, &A.ctl->fe[0]);
+        warp_append_capped(A, slot, buf, want, (int32_t)e, s, r_next, &A.ctl->pfe[np % 3]);
     }
-    return grid_barrier(&A.ctl->g, gridDim.x);
+    np++;
+    if (!grid_barrier(&A.ctl->g, gridDim.x)) return false;
+    return ld_cg_u64(&A.ctl->pfe[(np + 2) % 3]) > 0;
 }
 
 // Item windows: slot cb lies in item i0 (first slot base0); items i0+1.. start
@@ -603,7 +664,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
         ok = level_transition(A, 0, ntrans++, np, &l);
     } else {
         l = A.fixed_level;
-        ok = fixed_start(A, l);
+        ok = fixed_collect(A, l, 0, np);
     }
     if (!ok) {
         if (master) A.ctl->rounds = 0;
@@ -635,7 +696,13 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
         // fe[(r+1) % 3] is only written by sub-round r (level changes count
         // into pfe), and cleared again at the top of sub-round r+2
         if (ld_cg_u64(&A.ctl->fe[(r + 1) % 3]) == 0) {
-            if (A.mode != 0) break;
+            if (A.mode != 0) {
+                // k-truss search: the next batch of low-support edges, if any
+                if (!fixed_collect(A, l, r + 1, np)) break;
+                t_mark = globaltimer_ns();
+                r++;
+                continue;
+            }
             int32_t nl;
             const bool more = level_transition(A, r + 1, ntrans++, np, &nl);
             if (master) A.ctl->t_trans += globaltimer_ns() - t_b;
@@ -855,6 +922,13 @@ void prof_mark(int phase, cudaStream_t st);
 static long long g_peel_deadline_ns = 0;
 void set_peel_deadline(long long ns) { g_peel_deadline_ns = ns; }
 
+// Test hook: lower the k-truss collection batch limits (<= 0: the defaults).
+static long long g_fixed_item_cap = 0, g_fixed_cand_cap = 0;
+void set_fixed_caps(long long items, long long cands) {
+    g_fixed_item_cap = items;
+    g_fixed_cand_cap = cands;
+}
+
 // A grid barrier that one block never reaches: the others wait limit_ns, then
 // leave with TDT_ERR_TIMEOUT in ctl->status (the test of the bounded waits).
 __global__ void barrier_probe_kernel(GridCtl* ctl, unsigned long long limit_ns) {
@@ -1061,6 +1135,10 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     A.mode = mode == 0 ? 0 : 1;
     A.fixed_level = fixed_level;
     A.deadline_ns = g_peel_deadline_ns > 0 ? (unsigned long long)g_peel_deadline_ns : kPeelDeadlineNs;
+    A.fixed_item_cap = g_fixed_item_cap > 0 && (unsigned long long)g_fixed_item_cap < kFixedItemCap
+                           ? (unsigned long long)g_fixed_item_cap : kFixedItemCap;
+    A.fixed_cand_cap = g_fixed_cand_cap > 0 && (unsigned long long)g_fixed_cand_cap < kFixedCandCap
+                           ? (unsigned long long)g_fixed_cand_cap : kFixedCandCap;
     A.ctl = L.ctl;
     if (di.sms * occ > 4096) occ = 4096 / di.sms;
     dim3 grid(di.sms * occ), block(kPeelBlock);

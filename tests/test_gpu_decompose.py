@@ -247,3 +247,23 @@ def test_level_gaps_vs_oracle():
     pairs = np.concatenate(edges).astype(np.int32)
     pairs = rng.permutation(base + n).astype(np.int32)[pairs]
     _oracle_check(pairs)
+
+
+@pytest.mark.parametrize("caps", [(64, 1 << 30), (1 << 20, 300), (1, 1)])
+@pytest.mark.parametrize("lists", [True, False])
+def test_ktruss_search_in_small_batches(caps, lists):
+    """k-truss search whose starting frontier is queued a few edges (or a few
+    candidate slots) per sub-round: the same edge sets as without batching."""
+    from tdtdecomposition_gb300 import _lib
+    L = _lib.load()
+    s, d = G.rmat_edges(11, 16 << 11, seed=21)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
+    g = graph_of(rows, cols, rp)
+    truss = T.truss_decompose(g).truss.cpu().numpy()
+    L.tdt_set_ktruss_batch_caps(*caps)
+    try:
+        for k in (3, 4, 6, int(truss.max()), int(truss.max()) + 1):
+            m = T.ktruss_search(g, k, lists=lists).cpu().numpy()
+            assert np.array_equal(m, truss >= k), (caps, k)
+    finally:
+        L.tdt_set_ktruss_batch_caps(0, 0)
