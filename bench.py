@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--skewed", action="store_true",
+                    help="also run the skewed Chung-Lu graph (n=2^25): triangle count, decomposition, k-truss")
+    ap.add_argument("--skewed-log2n", type=int, default=25)
     return ap.parse_args()
 
 
@@ -264,6 +267,51 @@ def bench_batched(dev, steps, warmup, num_graphs=4096):
                            "note": "support, listing, the cooperative peel and outputs captured once, replayed"},
             "autotuned": {"warp_cap": tuned[0], "heavy_cap": tuned[1], "lists": tuned[2]},
             "host_generation_s": t_gen, "results_identical_to_plain": True}
+
+
+# ---------------------------------------------------------------- skewed single graph
+def bench_skewed(dev, log2n=25):
+    """Chung-Lu power law (exponent 2.1, n = 2^log2n, mean degree 40, degree
+    cap 2^20, seed 2), generated, deduplicated and degree-oriented on the
+    GPU; triangle count, full decomposition (per-edge triangle lists when 24 T
+    bytes fit the device, else the search peel) and k-truss search at
+    k in {3, 8, kmax/2, kmax}, each checked against {e : truss(e) >= k}.
+    One run each (seconds to a minute)."""
+    import torch
+    from tdtdecomposition_gb300 import generators as G, truss as T
+    from tdtdecomposition_gb300.preprocess import preprocess_edges
+    n = 1 << log2n
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t
+
+    (s, d), t_gen = timed(lambda: G.chung_lu_edges_device(n, seed=2, device=dev))
+    draws = s.numel()
+    (g, _), t_pre = timed(lambda: preprocess_edges(s, d))
+    del s, d
+    E, V = g.num_edges, g.num_vertices
+    ws = T.Workspace(dev)
+    T.triangle_count(g, workspace=ws)
+    tri, t_tc = timed(lambda: T.triangle_count(g, workspace=ws))
+    res, t_dec = timed(lambda: T.truss_decompose(g, workspace=ws))
+    truss = res.truss
+    kt = {}
+    for k in sorted({3, 8, res.kmax // 2, res.kmax}):
+        m, tk = timed(lambda: T.ktruss_search(g, k, workspace=ws))
+        if not torch.equal(m, truss >= k):
+            raise SystemExit("k-truss at k=%d differs from {e : truss(e) >= k}" % k)
+        kt[str(k)] = {"edges": int(m.sum()), "s": tk, "edges_per_s": E / tk}
+    return {"workload": "Chung-Lu n=2^%d, exponent 2.1, mean degree 40, degree cap 2^20, seed 2" % log2n,
+            "draws": draws, "V": V, "E": E, "triangles": tri, "kmax": res.kmax, "rounds": res.rounds,
+            "generate_s": t_gen, "preprocess_s": t_pre, "preprocess_draws_per_s": draws / t_pre,
+            "triangle_count_s": t_tc, "triangle_count_edges_per_s": E / t_tc,
+            "decompose_s": t_dec, "value": E / t_dec, "unit": UNIT,
+            "peel_mode": "lists" if res.listed else "search (24 T bytes of lists exceed the device budget)",
+            "ktruss": kt, "ktruss_equals_truss_ge_k": True}
 
 
 # ---------------------------------------------------------------- served workload
@@ -514,6 +562,8 @@ def main_ours(args):
         line["batched"] = bench_batched(dev, args.steps, args.warmup)
     if not args.no_served:
         line["served"] = bench_served(dev)
+    if args.skewed:
+        line["skewed"] = bench_skewed(dev, args.skewed_log2n)
     if not args.no_cpu_baseline:
         sc = cpu_sample_scale(args, 1)
         Ec, Vc, times, threads = cpu_decompose_sample(sc, 1)
