@@ -129,3 +129,122 @@ def k_truss(graph, n_cut, num_v, cpu_flow=False, compact_threshold=1000000):
                 l += 1
                 e_curr = torch.where(support == l)[0]
     return l + 2, e_truss, torch.tensor(ptr_truss, dtype=torch.int32)
+
+
+def all_affect_support_not_win(e_affect, graph, n_cut, mask, l, n_mark, support, windows_high, in_windows_mask,
+                               buff_index, buf_size):
+    """multigpu_truss_pre4.py:62-66 (the pybind names *_notwin)."""
+    if n_cut > 1:
+        tt.sub_AllAffectedSupport_tilenotwin(e_affect, graph.rows, graph.columns, graph.row_ptr, n_cut, mask, l,
+                                             n_mark, support, windows_high, in_windows_mask, buff_index, buf_size)
+    else:
+        tt.sub_AllAffectedSupport_notwin(e_affect, graph.rows, graph.columns, graph.row_ptr, mask, l, n_mark,
+                                         support, windows_high, in_windows_mask, buff_index, buf_size)
+
+
+def k_truss_windowed(graph, n_cut, num_v, windows_skip=16, compact_threshold=10000000):
+    """The support-window flow of demo_truss/multigpu_truss_pre4.py:75-199.
+
+    Edges whose support lies in the window [l, windows_high) are kept in a
+    buffer (buff_index[:buf_size]); the *_notwin peel update appends every edge
+    whose support falls into the window, so a new level's frontier is found in
+    the buffer instead of all edges, and the window moves up by windows_skip
+    levels when l reaches its top.  Mutates graph like the reference.
+    Returns (kmax, e_truss, ptr_truss): ptr_truss[j]..ptr_truss[j+1] are the
+    edges of level j+1 (truss number j+3); support-0 edges are left out.
+    Within a sub-round the order of e_truss follows the buffer, whose appends
+    are concurrent, so only the per-level sets are deterministic."""
+    dev = graph.device
+    support = support_computing(graph.rows, graph.columns, graph.row_ptr, n_cut)
+    e_truss = torch.zeros(0, dtype=torch.int32, device=dev)
+    ptr_truss = [0]
+    l = 1
+    edges = torch.arange(graph.columns.shape[0], dtype=torch.int32, device=dev)
+    e_mask = support.bool()
+    edges = edges[e_mask]
+    support = support[e_mask]
+    graph.columns = graph.columns[e_mask]
+    graph.rows = graph.rows[e_mask]
+    graph.row_ptr = update_row_ptr(e_mask, graph.row_ptr)
+    E = graph.columns.shape[0]
+    if E == 0:  # the reference loops forever here (no triangle)
+        return 2, e_truss, torch.tensor(ptr_truss, dtype=torch.int32)
+    edges_curr = torch.arange(E, dtype=torch.int32, device=dev)
+    buff_index = torch.zeros(E, dtype=torch.int32, device=dev)
+    buf_size = torch.zeros(1, dtype=torch.int32, device=dev)
+    windows_high = l + windows_skip
+
+    def fill_window(lo):
+        nonlocal in_windows_mask
+        in_windows_mask = (support >= lo) & (support < windows_high)
+        buff = edges_curr[in_windows_mask]
+        buf_size[0] = buff.shape[0]
+        buff_index[: buff.shape[0]] = buff
+
+    def frontier():
+        b = buff_index[: int(buf_size[0])].long()
+        return b[support[b] == l].to(torch.int32)
+
+    in_windows_mask = None
+    fill_window(0)
+    e_curr = frontier()
+
+    def next_level():
+        nonlocal l, windows_high, e_curr
+        e = e_curr
+        while e.shape[0] == 0:
+            ptr_truss.append(ptr_truss[-1])
+            l += 1
+            if l == windows_high:
+                windows_high = l + windows_skip
+                fill_window(l)
+            e = frontier()
+        e_curr = e
+
+    next_level()
+    peeled = 0
+    e_mask = torch.ones(E, dtype=torch.bool, device=dev)
+    while True:
+        e_truss = torch.cat([e_truss, edges[e_curr.long()]])
+        p = torch.unique(graph.rows[e_curr.long()])
+        mask_v = torch.zeros(num_v, dtype=torch.bool, device=dev)
+        mask_v[p] = True
+        mask = mask_v[graph.columns.long()]  # index -1 reads the last vertex, as in Python
+        p_c = _batched_csr_selection(graph.row_ptr[p * n_cut], graph.row_ptr[p * n_cut + n_cut])
+        mask[p_c] = e_mask[p_c]
+        e_affect = edges_curr[mask]
+        e_mask[e_curr.long()] = False
+        n_mark = torch.zeros(graph.columns.shape[0], dtype=torch.bool, device=dev)
+        all_affect_support_not_win(e_affect, graph, n_cut, e_mask, l, n_mark, support, windows_high,
+                                   in_windows_mask, buff_index, buf_size)
+        graph.columns[e_curr.long()] = -1
+        peeled += e_curr.shape[0]
+        if peeled > compact_threshold:
+            support = support[e_mask]
+            graph.columns = graph.columns[e_mask]
+            graph.rows = graph.rows[e_mask]
+            edges = edges[e_mask]
+            graph.row_ptr = update_row_ptr(e_mask, graph.row_ptr)
+            in_windows_mask = in_windows_mask[e_mask]
+            peeled = 0
+            edges_curr = torch.arange(graph.columns.shape[0], dtype=torch.int32, device=dev)
+            buff_index = torch.zeros(graph.columns.shape[0], dtype=torch.int32, device=dev)
+            buff = edges_curr[in_windows_mask]
+            buf_size[0] = buff.shape[0]
+            buff_index[: buff.shape[0]] = buff
+            n_mark = n_mark[e_mask]
+            e_mask = torch.ones(graph.columns.shape[0], dtype=torch.bool, device=dev)
+        e_curr = edges_curr[n_mark]
+        if peeled + e_curr.shape[0] == graph.columns.shape[0]:
+            e_truss = torch.cat([e_truss, edges[e_curr.long()]])
+            ptr_truss.append(e_truss.shape[0])
+            break
+        if e_curr.shape[0] == 0:
+            ptr_truss.append(e_truss.shape[0])
+            l += 1
+            if l == windows_high:
+                windows_high = l + windows_skip
+                fill_window(l)
+            e_curr = frontier()
+            next_level()
+    return l + 2, e_truss, torch.tensor(ptr_truss, dtype=torch.int32)

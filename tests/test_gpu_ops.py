@@ -220,3 +220,23 @@ def test_reference_flow_with_compaction():
     kmax, et, pt = flow.k_truss(g, 2, V, compact_threshold=0)
     assert kmax == int(d["sg_kmax2"])
     assert np.array_equal(host(et), d["sg_e_truss2"])
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("n_cut,skip,compact", [(1, 16, 10000000), (2, 16, 10000000), (2, 3, 10000000), (2, 4, 0)])
+def test_windowed_flow_on_dropin_ops(name, n_cut, skip, compact):
+    """The support-window flow of multigpu_truss_pre4.py over the *_notwin
+    operators: the reference's kmax, per-level peel sets and level offsets
+    (the order inside a sub-round follows the concurrently filled window
+    buffer); small windows and compaction on every round included."""
+    d = GD.load(name)
+    V = d["ref_vertices"].shape[0]
+    g = CSRCOO(columns=cu(d["ref_cols"]), row_ptr=cu(d["ref_rp_tiled%d" % n_cut]), rows=cu(d["ref_rows"]))
+    kmax, et, pt = flow.k_truss_windowed(g, n_cut, V, windows_skip=skip, compact_threshold=compact)
+    ref_et, ref_pt = d["sg_e_truss2"], d["sg_ptr_truss2"]
+    assert kmax == int(d["sg_kmax2"])
+    assert np.array_equal(pt.numpy(), ref_pt)
+    et = host(et)
+    for j in range(len(ref_pt) - 1):
+        a, b = ref_pt[j], ref_pt[j + 1]
+        assert np.array_equal(np.sort(et[a:b]), np.sort(ref_et[a:b])), j
