@@ -200,6 +200,94 @@ int tdt_sub_affected_support_tile(const int32_t *sub_rows, const int32_t *sub_co
                                   const uint8_t *mark, int32_t *sub_support, int64_t num_edges,
                                   tdt_stream_t stream);
 
+/* Research-variant operators (the reference's `tensor_original` and
+ * `undirected` drivers; none is on the `--cuda` flow).  Row-pointer arrays are
+ * int32, as the reference's ops read them; every list is sorted ascending
+ * without repeated keys (the reference's merge walk relies on it).
+ *
+ * segment_isinis_m (myhpu_extension.cpp:255-265; kernel.cu:687-737): for each
+ * row r < num_rows, the positions of the values rows r of a and b share, -1
+ * excepted, are set in mask1 (over a_columns) and mask2 (over b_columns).
+ * Both row-pointer arrays hold num_rows + 1 entries.
+ * segment_isinmm (myhpu_extension.cpp:555-565; kernel.cu:1555-1607): the same
+ * without the -1 exception. */
+int tdt_segment_isinis_m(const int32_t *a_columns, int64_t a_len, const int32_t *a_row_ptr,
+                         const int32_t *b_columns, int64_t b_len, const int32_t *b_row_ptr,
+                         int64_t num_rows, uint8_t *mask1, uint8_t *mask2, tdt_stream_t stream);
+int tdt_segment_isinmm(const int32_t *u_clos, int64_t u_len, const int32_t *v_clos, int64_t v_len,
+                       const int32_t *uptr, const int32_t *vptr, int64_t num_rows, uint8_t *u_mask,
+                       uint8_t *v_mask, tdt_stream_t stream);
+
+/* sub_suppport_affect (myhpu_extension.cpp:284-296; kernel.cu:739-805): for
+ * triangle i of a current edge e_curr_rep[i] with partner edges left_nbr[i]
+ * and right_nbr[i] (mask1/mask2: that partner takes part): both flagged ->
+ * both lose one; left only -> left loses one when e_curr_rep[i] < right;
+ * right only -> right loses one when e_curr_rep[i] < left.  Every decremented
+ * edge is set in e_affect_mask.  l is accepted and unused, as in the
+ * reference. */
+int tdt_sub_suppport_affect(const int32_t *left_nbr, const int32_t *right_nbr, const int32_t *e_curr_rep,
+                            int64_t num_triangles, int32_t *support, int64_t num_edges,
+                            const uint8_t *mask1, const uint8_t *mask2, uint8_t *e_affect_mask,
+                            int32_t l, tdt_stream_t stream);
+
+/* Oriented / undirected peel updates (myhpu_extension.cpp:316-539;
+ * kernel.cu:808-1551).  For each current edge e = (rows[e], columns[e]) and
+ * tile k < n_cut (1 for the untiled forms), the third vertices of its
+ * triangles are the keys two lists share:
+ *   peeling_undirect  symmetric adjacency of both ends (columns_g, edge ids
+ *                     edges_id_nbr, offsets row_ptr[v * n_cut + k]);
+ *   peeling_direct_oo out-lists of both ends (columns, offsets row_ptr);
+ *   peeling_direct_ii in-lists of both ends (edge ids r_edges grouped by head,
+ *                     keys rows[r_edges[i]], offsets re_ptr);
+ *   peeling_direct_oi out-list of the tail, in-list of the head.
+ * A shared key whose two edges e2 (first list) and e3 (second) are both in
+ * e_mask: neither in in_curr -> both lose one; only e3 in in_curr -> e2 loses
+ * one (undirect: when e < e3; ii: never); only e2 in in_curr -> e3 loses one
+ * (oo always; undirect when e < e2; ii, oi never).  An edge whose support
+ * goes from l + 1 to l is set in n_mark (the reference's op hands l + 1 to its
+ * kernel; pass the level l here as there).  Decrements are exact atomics, so
+ * supports and n_mark do not depend on thread order. */
+int tdt_peeling_undirect(const int32_t *e_curr, int64_t n_curr, const int32_t *rows,
+                         const int32_t *columns, const int32_t *columns_g, const int32_t *row_ptr,
+                         int64_t row_ptr_len, const int32_t *edges_id_nbr, int64_t g_len,
+                         int32_t *support, const uint8_t *e_mask, uint8_t *n_mark,
+                         const uint8_t *in_curr, int32_t l, int64_t num_edges, tdt_stream_t stream);
+int tdt_peeling_undirect_tile(const int32_t *e_curr, int64_t n_curr, const int32_t *rows,
+                              const int32_t *columns, const int32_t *columns_g, const int32_t *row_ptr,
+                              int64_t row_ptr_len, const int32_t *edges_id_nbr, int64_t g_len,
+                              int32_t *support, const uint8_t *e_mask, uint8_t *n_mark,
+                              const uint8_t *in_curr, int32_t l, int32_t n_cut, int64_t num_edges,
+                              tdt_stream_t stream);
+int tdt_peeling_direct_oo(const int32_t *e_curr, int64_t n_curr, const int32_t *rows, const int32_t *columns,
+                          const int32_t *row_ptr, int64_t row_ptr_len, int32_t *support,
+                          const uint8_t *e_mask, uint8_t *n_mark, const uint8_t *in_curr, int32_t l,
+                          int64_t num_edges, tdt_stream_t stream);
+int tdt_peeling_direct_tile_oo(const int32_t *e_curr, int64_t n_curr, const int32_t *rows,
+                               const int32_t *columns, const int32_t *row_ptr, int64_t row_ptr_len,
+                               int32_t *support, const uint8_t *e_mask, uint8_t *n_mark,
+                               const uint8_t *in_curr, int32_t l, int32_t n_cut, int64_t num_edges,
+                               tdt_stream_t stream);
+int tdt_peeling_direct_ii(const int32_t *e_curr, int64_t n_curr, const int32_t *rows, const int32_t *columns,
+                          const int32_t *r_edges, const int32_t *re_ptr, int64_t re_ptr_len,
+                          int32_t *support, const uint8_t *e_mask, uint8_t *n_mark,
+                          const uint8_t *in_curr, int32_t l, int64_t num_edges, tdt_stream_t stream);
+int tdt_peeling_direct_tile_ii(const int32_t *e_curr, int64_t n_curr, const int32_t *rows,
+                               const int32_t *columns, const int32_t *r_edges, const int32_t *re_ptr,
+                               int64_t re_ptr_len, int32_t *support, const uint8_t *e_mask,
+                               uint8_t *n_mark, const uint8_t *in_curr, int32_t l, int32_t n_cut,
+                               int64_t num_edges, tdt_stream_t stream);
+int tdt_peeling_direct_oi(const int32_t *e_curr, int64_t n_curr, const int32_t *rows, const int32_t *columns,
+                          const int32_t *row_ptr, int64_t row_ptr_len, const int32_t *r_edges,
+                          const int32_t *re_ptr, int64_t re_ptr_len, int32_t *support,
+                          const uint8_t *e_mask, uint8_t *n_mark, const uint8_t *in_curr, int32_t l,
+                          int64_t num_edges, tdt_stream_t stream);
+int tdt_peeling_direct_tile_oi(const int32_t *e_curr, int64_t n_curr, const int32_t *rows,
+                               const int32_t *columns, const int32_t *row_ptr, int64_t row_ptr_len,
+                               const int32_t *r_edges, const int32_t *re_ptr, int64_t re_ptr_len,
+                               int32_t *support, const uint8_t *e_mask, uint8_t *n_mark,
+                               const uint8_t *in_curr, int32_t l, int32_t n_cut, int64_t num_edges,
+                               tdt_stream_t stream);
+
 /* =====================================================================
  * Whole-path entry points (the device-resident hot path).
  * ===================================================================== */

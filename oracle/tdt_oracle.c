@@ -479,3 +479,100 @@ ORC_API int orc_num_threads(void) {
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------ */
+/* Research-variant operators (sequential merge walks)                  */
+/* ------------------------------------------------------------------ */
+/* The decrements of these operators commute, so one thread walking the work
+ * items in order ends in the same supports and marks as the reference's
+ * thread-per-item kernels. */
+
+/* myhpu_extension_kernel.cu:687-713 (checkElementsTwoPtrIsInIs, skip_neg1 = 1)
+ * and :1555-1583 (segmentIsinmmKernel, skip_neg1 = 0): per row, a merge walk of
+ * the two sorted rows flags the positions of equal values. */
+ORC_API void orc_rows_isin_mask(const int32_t *a, const int32_t *ap, const int32_t *b, const int32_t *bp,
+                                int64_t rows, uint8_t *m1, uint8_t *m2, int skip_neg1) {
+    for (int64_t r = 0; r < rows; r++) {
+        int32_t i = ap[r], ie = ap[r + 1], j = bp[r], je = bp[r + 1];
+        while (i < ie && j < je) {
+            int32_t x = a[i], y = b[j];
+            if (x == y && !(skip_neg1 && x == -1)) {
+                m1[i++] = 1;
+                m2[j++] = 1;
+            } else if (x < y) {
+                i++;
+            } else {
+                j++;
+            }
+        }
+    }
+}
+
+/* myhpu_extension_kernel.cu:739-779 (checkTriangleSupportSub). */
+ORC_API void orc_support_affect(const int32_t *left, const int32_t *right, const int32_t *cur, int64_t n,
+                                int32_t *support, const uint8_t *m1, const uint8_t *m2, uint8_t *affect) {
+    for (int64_t i = 0; i < n; i++) {
+        int32_t a = left[i], b = right[i], c = cur[i];
+        if (m1[i] && m2[i]) {
+            support[a]--; support[b]--; affect[a] = 1; affect[b] = 1;
+        } else if (m1[i]) {
+            if (c < b) { support[a]--; affect[a] = 1; }
+        } else if (m2[i]) {
+            if (c < a) { support[b]--; affect[b] = 1; }
+        }
+    }
+}
+
+static void orc_dec_mark(int32_t *support, uint8_t *n_mark, int32_t x, int32_t lp1) {
+    if (support[x]-- == lp1) n_mark[x] = 1;
+}
+
+/* myhpu_extension_kernel.cu:808-1551 (peeling_edges_undirect, _direct_oo,
+ * _direct_ii, _direct_oi and their _tile forms).  variant: 0 undirect, 1 oo,
+ * 2 ii, 3 oi; lp1 = the level + 1 (what the reference's op hands its kernel);
+ * n_cut = 1 for the untiled forms.  List A belongs to the tail rows[e], list B
+ * to the head columns[e]. */
+ORC_API void orc_peel_op(int variant, const int32_t *e_curr, int64_t n_curr, const int32_t *rows,
+                         const int32_t *columns, const int32_t *row_ptr, const int32_t *r_edges,
+                         const int32_t *re_ptr, const int32_t *columns_g, const int32_t *edges_id_nbr,
+                         int32_t *support, const uint8_t *e_mask, uint8_t *n_mark, const uint8_t *in_curr,
+                         int32_t lp1, int32_t n_cut) {
+    for (int64_t t = 0; t < n_curr * n_cut; t++) {
+        int32_t e = e_curr[t / n_cut], k = (int32_t)(t % n_cut);
+        int64_t u = (int64_t)rows[e] * n_cut + k, v = (int64_t)columns[e] * n_cut + k;
+        /* list A: out (oo, oi), in (ii) or symmetric (undirect); list B: out (oo), in (ii, oi) or symmetric */
+        const int32_t *pa = variant == 2 ? re_ptr : row_ptr;
+        const int32_t *pb = (variant == 2 || variant == 3) ? re_ptr : row_ptr;
+        int32_t i = pa[u], ie = pa[u + 1], j = pb[v], je = pb[v + 1];
+        while (i < ie && j < je) {
+            int32_t ka, kb, e2, e3;
+            if (variant == 0) { ka = columns_g[i]; e2 = edges_id_nbr[i]; }
+            else if (variant == 2) { e2 = r_edges[i]; ka = rows[e2]; }
+            else { ka = columns[i]; e2 = i; }
+            if (variant == 0) { kb = columns_g[j]; e3 = edges_id_nbr[j]; }
+            else if (variant == 1) { kb = columns[j]; e3 = j; }
+            else { e3 = r_edges[j]; kb = rows[e3]; }
+            if (ka == kb) {
+                if (e_mask[e2] && e_mask[e3]) {
+                    int f2 = in_curr[e2], f3 = in_curr[e3];
+                    if (!f2 && !f3) {
+                        orc_dec_mark(support, n_mark, e2, lp1);
+                        orc_dec_mark(support, n_mark, e3, lp1);
+                    } else if (!f2 && f3) {
+                        if (variant == 1 || variant == 3 || (variant == 0 && e < e3))
+                            orc_dec_mark(support, n_mark, e2, lp1);
+                    } else if (f2 && !f3) {
+                        if (variant == 1 || (variant == 0 && e < e2))
+                            orc_dec_mark(support, n_mark, e3, lp1);
+                    }
+                }
+                i++;
+                j++;
+            } else if (ka < kb) {
+                i++;
+            } else {
+                j++;
+            }
+        }
+    }
+}

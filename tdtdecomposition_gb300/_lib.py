@@ -53,6 +53,30 @@ _SIGS = [
     ("tdt_sub_affected_support", ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr]),
     ("tdt_sub_affected_support_tile", ctypes.c_int,
      [c_ptr, c_ptr, c_ptr, c_i64, c_i32, c_ptr, c_ptr, c_i64, c_ptr]),
+    ("tdt_segment_isinis_m", ctypes.c_int, [c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_ptr, c_ptr]),
+    ("tdt_segment_isinmm", ctypes.c_int, [c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_ptr]),
+    ("tdt_sub_suppport_affect", ctypes.c_int,
+     [c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_i32, c_ptr]),
+    ("tdt_peeling_undirect", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i64,
+      c_ptr]),
+    ("tdt_peeling_undirect_tile", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i32,
+      c_i64, c_ptr]),
+    ("tdt_peeling_direct_oo", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i64, c_ptr]),
+    ("tdt_peeling_direct_tile_oo", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i32, c_i64, c_ptr]),
+    ("tdt_peeling_direct_ii", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i64, c_ptr]),
+    ("tdt_peeling_direct_tile_ii", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i32, c_i64, c_ptr]),
+    ("tdt_peeling_direct_oi", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i64,
+      c_ptr]),
+    ("tdt_peeling_direct_tile_oi", ctypes.c_int,
+     [c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i32,
+      c_i64, c_ptr]),
     ("tdt_preprocess_workspace_bytes", c_size, [c_i64, c_i64]),
     ("tdt_preprocess", ctypes.c_int,
      [c_ptr, c_ptr, c_i64, c_i64, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_size, c_ptr]),

@@ -248,3 +248,177 @@ def k_truss_windowed(graph, n_cut, num_v, windows_skip=16, compact_threshold=100
             e_curr = frontier()
             next_level()
     return l + 2, e_truss, torch.tensor(ptr_truss, dtype=torch.int32)
+
+
+# ------------------------------------------------------------------ undirected-graph drivers
+# demo_truss/undirected/truss_undirect_cuda.py and truss_undirect_cuda2.py: the
+# same level / sub-round peel as k_truss, but every current edge removes its
+# triangles itself through the oriented (peeling_direct_oo/ii/oi) or the
+# symmetric (peeling_undirect) update, so no affected-edge gather is needed.
+# Edges in no triangle are dropped before the peel and appear in no level;
+# level l (from 1) holds the edges of truss number l + 2.  The input graph is
+# left untouched.
+
+def _in_list_sizes(rows, cols, r_edges, num_v, n_cut):
+    if n_cut > 1:
+        block = rows[r_edges].to(torch.int64) // (num_v // n_cut + 1) + cols[r_edges].to(torch.int64) * n_cut
+    else:
+        block = cols[r_edges].to(torch.int64)
+    return torch.bincount(block, minlength=num_v * n_cut).to(torch.int32)
+
+
+def preprocess_direct(graph, n_cut):
+    """truss_undirect_cuda2.py:118-141: returns the (tiled) out-list offsets,
+    r_edges (edge ids stably sorted by head) and their (tiled) offsets re_ptr,
+    all int32."""
+    from .graph import tiling_row_ptr
+    num_v = graph.num_vertices
+    row_ptr = tiling_row_ptr(graph, n_cut) if n_cut > 1 else graph.row_ptr.to(torch.int32)
+    r_edges = torch.argsort(graph.columns, stable=True).to(torch.int32)
+    size_r = _in_list_sizes(graph.rows, graph.columns, r_edges, num_v, n_cut)
+    re_ptr = torch.cat([torch.zeros(1, dtype=torch.int32, device=size_r.device), size_r.cumsum(0, dtype=torch.int32)])
+    return row_ptr, r_edges, re_ptr
+
+
+def preprocess_undirect(graph, n_cut_s, n_cut):
+    """truss_undirect_cuda.py:80-121: returns (directed_ptr, columns_g,
+    edges_id_nbr, row_ptr_g).  directed_ptr: the out-list offsets tiled by
+    n_cut_s for the support count; slot v*n_cut+k of the symmetric adjacency
+    lists the in-neighbours of v in tile k, then its out-neighbours in tile k."""
+    from .graph import tiling_row_ptr
+    num_v = graph.num_vertices
+    dev = graph.columns.device
+    directed_ptr = tiling_row_ptr(graph, n_cut_s) if n_cut_s > 1 else graph.row_ptr.to(torch.int32)
+    r_edge = torch.argsort(graph.columns, stable=True).to(torch.int32)
+    size_r = _in_list_sizes(graph.rows, graph.columns, r_edge, num_v, n_cut)
+    out_ptr = tiling_row_ptr(graph, n_cut) if n_cut > 1 else graph.row_ptr.to(torch.int32)
+    ptr_g = out_ptr.to(torch.int64).clone()
+    ptr_g[1:] += size_r.cumsum(0)
+    E = graph.columns.shape[0]
+    columns_g = torch.zeros(2 * E, dtype=torch.int32, device=dev)
+    edges_id_nbr = torch.zeros(2 * E, dtype=torch.int32, device=dev)
+    out_idx = _batched_csr_selection(ptr_g[:-1] + size_r, ptr_g[1:])
+    edges_id_nbr[out_idx] = torch.arange(E, dtype=torch.int32, device=dev)
+    columns_g[out_idx] = graph.columns
+    in_idx = _batched_csr_selection(ptr_g[:-1], ptr_g[:-1] + size_r)
+    edges_id_nbr[in_idx] = r_edge
+    columns_g[in_idx] = graph.rows[r_edge.to(torch.int64)]
+    return directed_ptr, columns_g, edges_id_nbr, ptr_g.to(torch.int32)
+
+
+def _e_map(keep):
+    m = torch.zeros(keep.shape[0] + 1, dtype=torch.int32, device=keep.device)
+    m[1:] = torch.cumsum(keep.int(), 0, dtype=torch.int32)
+    return m
+
+
+def _undirected_peel(support, edges, num_edges, peel, compact, compact_threshold):
+    dev = support.device
+    e_truss = []
+    ptr_truss = [0]
+    l = 1
+    if support.shape[0] == 0:  # the reference's level search never ends here
+        return 2, torch.zeros(0, dtype=torch.int32, device=dev), torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def next_level(support, l):
+        in_curr = support == l
+        while not bool(in_curr.any()):
+            ptr_truss.append(ptr_truss[-1])
+            l += 1
+            in_curr = support == l
+        return l, in_curr
+
+    def done(l):
+        e = torch.cat(e_truss) if e_truss else torch.zeros(0, dtype=torch.int32, device=dev)
+        return l + 2, e, torch.tensor(ptr_truss, dtype=torch.int32, device=dev)
+
+    l, in_curr = next_level(support, l)
+    e_curr = torch.where(in_curr)[0].to(torch.int32)
+    e_mask = torch.ones(support.shape[0], dtype=torch.bool, device=dev)
+    count, n_out = 0, 0
+    while True:
+        while e_curr.shape[0] != 0:
+            e_truss.append(edges[e_curr.long()])
+            n_out += e_curr.shape[0]
+            n_mark = torch.zeros(support.shape[0], dtype=torch.bool, device=dev)
+            peel(e_curr, support, e_mask, n_mark, in_curr, l)
+            e_mask[e_curr.long()] = False
+            count += e_curr.shape[0]
+            in_curr = n_mark
+            e_curr = torch.where(n_mark)[0].to(torch.int32)
+            if count + e_curr.shape[0] == num_edges():
+                e_truss.append(edges[e_curr.long()])
+                ptr_truss.append(n_out + e_curr.shape[0])
+                return done(l)
+        if count > compact_threshold:
+            support, edges = compact(e_mask, support, edges)
+            count = 0
+            e_mask = torch.ones(support.shape[0], dtype=torch.bool, device=dev)
+        ptr_truss.append(n_out)
+        l, in_curr = next_level(support, l + 1)
+        e_curr = torch.where(in_curr)[0].to(torch.int32)
+
+
+def undirected_truss_direct(graph, row_ptr, r_edges, re_ptr, n_cut, compact_threshold=10000000):
+    """truss_undirect_cuda2.py:145-280 (undirected_truss) with the oriented
+    peel updates: returns (kmax, e_truss, ptr_truss).  row_ptr, r_edges, re_ptr
+    come from preprocess_direct(graph, n_cut)."""
+    g = {"rows": graph.rows, "cols": graph.columns, "rp": row_ptr, "r": r_edges, "re": re_ptr}
+    support = support_computing(g["rows"], g["cols"], g["rp"], n_cut)
+
+    def compact(keep, support, edges):
+        g["cols"], g["rows"] = g["cols"][keep], g["rows"][keep]
+        g["rp"] = update_row_ptr(keep, g["rp"])
+        e_map = _e_map(keep)
+        keep_r = keep[g["r"].long()]
+        g["r"] = e_map[g["r"][keep_r].long()]
+        g["re"] = update_row_ptr(keep_r, g["re"])
+        return support[keep], edges[keep]
+
+    edges = torch.arange(support.shape[0], dtype=torch.int32, device=support.device)
+    support, edges = compact(support.bool(), support, edges)
+    tile = n_cut > 1
+
+    def peel(e_curr, support, e_mask, n_mark, in_curr, l):
+        a = (e_curr, g["rows"], g["cols"])
+        t = (support, e_mask, n_mark, in_curr, l)
+        if tile:
+            tt.peeling_direct_tile_oo(*a, g["rp"], *t, n_cut)
+            tt.peeling_direct_tile_ii(*a, g["r"], g["re"], *t, n_cut)
+            tt.peeling_direct_tile_oi(*a, g["rp"], g["r"], g["re"], *t, n_cut)
+        else:
+            tt.peeling_direct_oo(*a, g["rp"], *t)
+            tt.peeling_direct_ii(*a, g["r"], g["re"], *t)
+            tt.peeling_direct_oi(*a, g["rp"], g["r"], g["re"], *t)
+
+    return _undirected_peel(support, edges, lambda: g["cols"].shape[0], peel, compact, compact_threshold)
+
+
+def undirected_truss_undirect(graph, columns_g, edges_id_nbr, directed_ptr, row_ptr_g, n_cut_s, n_cut,
+                              compact_threshold=10000000):
+    """truss_undirect_cuda.py:125-235 (undirected_truss) with the symmetric
+    peel update; inputs from preprocess_undirect(graph, n_cut_s, n_cut)."""
+    g = {"rows": graph.rows, "cols": graph.columns, "cg": columns_g, "nbr": edges_id_nbr, "pg": row_ptr_g}
+    support = support_computing(g["rows"], g["cols"], directed_ptr, n_cut_s)
+
+    def compact(keep, support, edges):
+        g["cols"], g["rows"] = g["cols"][keep], g["rows"][keep]
+        e_map = _e_map(keep)
+        keep_g = keep[g["nbr"].long()]
+        g["cg"] = g["cg"][keep_g]
+        g["nbr"] = e_map[g["nbr"][keep_g].long()]
+        g["pg"] = update_row_ptr(keep_g, g["pg"])
+        return support[keep], edges[keep]
+
+    edges = torch.arange(support.shape[0], dtype=torch.int32, device=support.device)
+    support, edges = compact(support.bool(), support, edges)
+
+    def peel(e_curr, support, e_mask, n_mark, in_curr, l):
+        if n_cut > 1:
+            tt.peeling_undirect_tile(e_curr, g["rows"], g["cols"], g["cg"], g["pg"], g["nbr"], support, e_mask,
+                                     n_mark, in_curr, l, n_cut)
+        else:
+            tt.peeling_undirect(e_curr, g["rows"], g["cols"], g["cg"], g["pg"], g["nbr"], support, e_mask, n_mark,
+                                in_curr, l)
+
+    return _undirected_peel(support, edges, lambda: g["cols"].shape[0], peel, compact, compact_threshold)

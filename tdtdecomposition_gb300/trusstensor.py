@@ -13,10 +13,9 @@ contiguous, sizes) and a bad call raises instead of reading out of bounds;
 CPU tensors raise (the reference dispatched those to OpenMP twins; this
 library has no CPU path).
 
-Operators of the reference's research variants that are outside the
-truss-decomposition hot path (undirected/oriented peeling kernels, the
-triangle-list and fusion-ablation kernels) are exported and raise
-NotImplementedError.
+The research-variant operators (segment_isinis_m, sub_suppport_affect,
+segment_isinmm and the undirected/oriented peel updates) are implemented too;
+their drivers are restated in ``flow.py``.
 """
 import torch
 
@@ -207,24 +206,155 @@ def sub_AffectedSupport_tile(sub_rows, sub_columns, sub_row_ptr, n_cut, mark, su
           _i32(sub_support, "sub_support"), sub_support.shape[0], _stream())
 
 
-# ------------------------------------------------------------------ outside the hot path
-def _not_on_path(name, where):
-    def op(*args, **kwargs):
-        raise NotImplementedError(
-            "trusstensor.%s (%s) belongs to the reference's research variants, not to the "
-            "truss-decomposition hot path this library replaces" % (name, where))
-    op.__name__ = name
-    return op
+# ------------------------------------------------------------------ research-variant operators
+def _rows_mask(fn, a_cols, a_ptr, b_cols, b_ptr, m1, m2):
+    _same_device(a_cols, a_ptr, b_cols, b_ptr, m1, m2)
+    n = max(a_ptr.shape[0] - 1, 0)
+    if b_ptr.shape[0] < n + 1:
+        raise ValueError("the second row-pointer array has %d entries, need %d" % (b_ptr.shape[0], n + 1))
+    if m1.shape[0] < a_cols.shape[0] or m2.shape[0] < b_cols.shape[0]:
+        raise ValueError("each mask needs one entry per value of its columns")
+    _call(fn, _i32(a_cols, "a_columns"), a_cols.shape[0], _i32(a_ptr, "a_row_ptr"), _i32(b_cols, "b_columns"),
+          b_cols.shape[0], _i32(b_ptr, "b_row_ptr"), n, _u8(m1, "mask1"), _u8(m2, "mask2"), _stream())
 
 
-segment_isinis_m = _not_on_path("segment_isinis_m", "kernel.cu:687-737")
-sub_suppport_affect = _not_on_path("sub_suppport_affect", "kernel.cu:739-805")
-peeling_undirect = _not_on_path("peeling_undirect", "kernel.cu:808-905")
-peeling_undirect_tile = _not_on_path("peeling_undirect_tile", "kernel.cu:908-1009")
-peeling_direct_oo = _not_on_path("peeling_direct_oo", "kernel.cu:1012-1093")
-peeling_direct_tile_oo = _not_on_path("peeling_direct_tile_oo", "kernel.cu:1096-1181")
-peeling_direct_ii = _not_on_path("peeling_direct_ii", "kernel.cu:1184-1272")
-peeling_direct_tile_ii = _not_on_path("peeling_direct_tile_ii", "kernel.cu:1275-1367")
-peeling_direct_oi = _not_on_path("peeling_direct_oi", "kernel.cu:1370-1457")
-peeling_direct_tile_oi = _not_on_path("peeling_direct_tile_oi", "kernel.cu:1460-1551")
-segment_isinmm = _not_on_path("segment_isinmm", "kernel.cu:1555-1607")
+def segment_isinis_m(a_columns, a_row_ptr, b_columns, b_row_ptr, mask1, mask2):
+    """myhpu_extension.cpp:255-265 (kernel.cu:687-737): per row r, set mask1/mask2
+    at the positions of the values rows r of a and b share (-1 excepted)."""
+    _rows_mask("tdt_segment_isinis_m", a_columns, a_row_ptr, b_columns, b_row_ptr, mask1, mask2)
+
+
+def segment_isinmm(u_clos, v_clos, uptr, vptr, u_mask, v_mask):
+    """myhpu_extension.cpp:555-565 (kernel.cu:1555-1607): segment_isinis_m
+    without the -1 exception."""
+    _same_device(u_clos, v_clos, uptr, vptr, u_mask, v_mask)
+    n = max(uptr.shape[0] - 1, 0)
+    if vptr.shape[0] < n + 1:
+        raise ValueError("vptr has %d entries, need %d" % (vptr.shape[0], n + 1))
+    if u_mask.shape[0] < u_clos.shape[0] or v_mask.shape[0] < v_clos.shape[0]:
+        raise ValueError("each mask needs one entry per value of its columns")
+    _call("tdt_segment_isinmm", _i32(u_clos, "u_clos"), u_clos.shape[0], _i32(v_clos, "v_clos"), v_clos.shape[0],
+          _i32(uptr, "uptr"), _i32(vptr, "vptr"), n, _u8(u_mask, "u_mask"), _u8(v_mask, "v_mask"), _stream())
+
+
+def sub_suppport_affect(left_nbr, right_nbr, e_curr_rep, support, mask1, mask2, e_affect_mask, l):
+    """myhpu_extension.cpp:284-296 (kernel.cu:739-805): per triangle i of
+    e_curr_rep[i], decrement the flagged partner edges (one flagged: only when
+    e_curr_rep[i] is below the other partner) and flag them in e_affect_mask."""
+    _same_device(left_nbr, right_nbr, e_curr_rep, support, mask1, mask2, e_affect_mask)
+    n = left_nbr.shape[0]
+    for name, t in (("right_nbr", right_nbr), ("e_curr_rep", e_curr_rep), ("mask1", mask1), ("mask2", mask2)):
+        if t.shape[0] < n:
+            raise ValueError("%s has %d entries, fewer than left_nbr's %d" % (name, t.shape[0], n))
+    if e_affect_mask.shape[0] < support.shape[0]:
+        raise ValueError("e_affect_mask needs one entry per edge")
+    _call("tdt_sub_suppport_affect", _i32(left_nbr, "left_nbr"), _i32(right_nbr, "right_nbr"),
+          _i32(e_curr_rep, "e_curr_rep"), n, _i32(support, "support"), support.shape[0], _u8(mask1, "mask1"),
+          _u8(mask2, "mask2"), _u8(e_affect_mask, "e_affect_mask"), int(l), _stream())
+
+
+def _peel_common(e_curr, rows, columns, support, e_mask, n_mark, in_curr, extra):
+    _same_device(e_curr, rows, columns, support, e_mask, n_mark, in_curr, *extra)
+    E = columns.shape[0]
+    for name, t in (("rows", rows), ("support", support), ("e_mask", e_mask), ("n_mark", n_mark),
+                    ("in_curr", in_curr)):
+        if t.shape[0] < E:
+            raise ValueError("%s has %d entries, fewer than the %d edges" % (name, t.shape[0], E))
+    return E, [_i32(e_curr, "e_curr"), e_curr.shape[0], _i32(rows, "rows"), _i32(columns, "columns")]
+
+
+def _tail(support, e_mask, n_mark, in_curr):
+    return [_i32(support, "support"), _u8(e_mask, "e_mask"), _u8(n_mark, "n_mark"), _u8(in_curr, "in_curr")]
+
+
+def _undirect(fn, e_curr, rows, columns, columns_g, row_ptr, edges_id_nbr, support, e_mask, n_mark, in_curr, l,
+              n_cut):
+    E, args = _peel_common(e_curr, rows, columns, support, e_mask, n_mark, in_curr,
+                           (columns_g, row_ptr, edges_id_nbr))
+    if edges_id_nbr.shape[0] < columns_g.shape[0]:
+        raise ValueError("edges_id_nbr needs one entry per value of columns_g")
+    args += [_i32(columns_g, "columns_g"), _i32(row_ptr, "row_ptr"), row_ptr.shape[0],
+             _i32(edges_id_nbr, "edges_id_nbr"), columns_g.shape[0]] + _tail(support, e_mask, n_mark, in_curr)
+    args += [int(l)] + ([] if n_cut is None else [int(n_cut)]) + [E, _stream()]
+    _call(fn, *args)
+
+
+def peeling_undirect(e_curr, rows, columns, columns_g, row_ptr, edges_id_nbr, support, e_mask, n_mark, in_curr, l):
+    """myhpu_extension.cpp:316-331 (kernel.cu:808-905): peel update over the
+    symmetric adjacency (columns_g, edges_id_nbr, row_ptr)."""
+    _undirect("tdt_peeling_undirect", e_curr, rows, columns, columns_g, row_ptr, edges_id_nbr, support, e_mask,
+              n_mark, in_curr, l, None)
+
+
+def peeling_undirect_tile(e_curr, rows, columns, columns_g, row_ptr, edges_id_nbr, support, e_mask, n_mark, in_curr,
+                          l, n_cut):
+    """myhpu_extension.cpp:348-363 (kernel.cu:908-1009): the tiled form."""
+    _undirect("tdt_peeling_undirect_tile", e_curr, rows, columns, columns_g, row_ptr, edges_id_nbr, support, e_mask,
+              n_mark, in_curr, l, n_cut)
+
+
+def _oo(fn, e_curr, rows, columns, row_ptr, support, e_mask, n_mark, in_curr, l, n_cut):
+    E, args = _peel_common(e_curr, rows, columns, support, e_mask, n_mark, in_curr, (row_ptr,))
+    args += [_i32(row_ptr, "row_ptr"), row_ptr.shape[0]] + _tail(support, e_mask, n_mark, in_curr)
+    args += [int(l)] + ([] if n_cut is None else [int(n_cut)]) + [E, _stream()]
+    _call(fn, *args)
+
+
+def peeling_direct_oo(e_curr, rows, columns, row_ptr, support, e_mask, n_mark, in_curr, l):
+    """myhpu_extension.cpp:377-390 (kernel.cu:1012-1093): third vertex in the
+    out-lists of both ends."""
+    _oo("tdt_peeling_direct_oo", e_curr, rows, columns, row_ptr, support, e_mask, n_mark, in_curr, l, None)
+
+
+def peeling_direct_tile_oo(e_curr, rows, columns, row_ptr, support, e_mask, n_mark, in_curr, l, n_cut):
+    """myhpu_extension.cpp:405-418 (kernel.cu:1096-1181)."""
+    _oo("tdt_peeling_direct_tile_oo", e_curr, rows, columns, row_ptr, support, e_mask, n_mark, in_curr, l, n_cut)
+
+
+def _check_r_edges(r_edges, E):
+    if r_edges.shape[0] < E:
+        raise ValueError("r_edges has %d entries, fewer than the %d edges" % (r_edges.shape[0], E))
+
+
+def _ii(fn, e_curr, rows, columns, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l, n_cut):
+    E, args = _peel_common(e_curr, rows, columns, support, e_mask, n_mark, in_curr, (r_edges, re_ptr))
+    _check_r_edges(r_edges, E)
+    args += [_i32(r_edges, "r_edges"), _i32(re_ptr, "re_ptr"), re_ptr.shape[0]] + _tail(support, e_mask, n_mark,
+                                                                                         in_curr)
+    args += [int(l)] + ([] if n_cut is None else [int(n_cut)]) + [E, _stream()]
+    _call(fn, *args)
+
+
+def peeling_direct_ii(e_curr, rows, columns, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l):
+    """myhpu_extension.cpp:432-446 (kernel.cu:1184-1272): third vertex in the
+    in-lists of both ends (r_edges grouped by head, offsets re_ptr)."""
+    _ii("tdt_peeling_direct_ii", e_curr, rows, columns, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l, None)
+
+
+def peeling_direct_tile_ii(e_curr, rows, columns, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l, n_cut):
+    """myhpu_extension.cpp:462-476 (kernel.cu:1275-1367)."""
+    _ii("tdt_peeling_direct_tile_ii", e_curr, rows, columns, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l,
+        n_cut)
+
+
+def _oi(fn, e_curr, rows, columns, row_ptr, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l, n_cut):
+    E, args = _peel_common(e_curr, rows, columns, support, e_mask, n_mark, in_curr, (row_ptr, r_edges, re_ptr))
+    _check_r_edges(r_edges, E)
+    args += [_i32(row_ptr, "row_ptr"), row_ptr.shape[0], _i32(r_edges, "r_edges"), _i32(re_ptr, "re_ptr"),
+             re_ptr.shape[0]] + _tail(support, e_mask, n_mark, in_curr)
+    args += [int(l)] + ([] if n_cut is None else [int(n_cut)]) + [E, _stream()]
+    _call(fn, *args)
+
+
+def peeling_direct_oi(e_curr, rows, columns, row_ptr, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l):
+    """myhpu_extension.cpp:492-507 (kernel.cu:1370-1457): third vertex in the
+    tail's out-list and the head's in-list."""
+    _oi("tdt_peeling_direct_oi", e_curr, rows, columns, row_ptr, r_edges, re_ptr, support, e_mask, n_mark, in_curr,
+        l, None)
+
+
+def peeling_direct_tile_oi(e_curr, rows, columns, row_ptr, r_edges, re_ptr, support, e_mask, n_mark, in_curr, l,
+                           n_cut):
+    """myhpu_extension.cpp:524-540 (kernel.cu:1460-1551)."""
+    _oi("tdt_peeling_direct_tile_oi", e_curr, rows, columns, row_ptr, r_edges, re_ptr, support, e_mask, n_mark,
+        in_curr, l, n_cut)

@@ -60,8 +60,15 @@ def test_operators_reject_cpu_tensors():
         tt.segment_isin2tile(x, x, torch.zeros(5, dtype=torch.int32), 2, x)
 
 
-def test_out_of_path_operators_raise():
-    with pytest.raises(NotImplementedError):
-        tt.peeling_direct_oo(None)
+def test_research_operators_check_their_arguments():
+    """The research-variant operators are real: CPU tensors are refused like
+    every other operator's (there is no CPU path)."""
+    x = torch.zeros(4, dtype=torch.int32)
+    b = torch.zeros(4, dtype=torch.bool)
+    with pytest.raises(TypeError):
+        tt.peeling_direct_oo(x, x, x, x, x, b, b, b, 1)
+    with pytest.raises(TypeError):
+        tt.segment_isinis_m(x, x, x, x, b, b)
+    assert all(not getattr(tt, n).__doc__ is None for n in tt.__all__)
     assert len([n for n in tt.__all__ if not n.endswith("_k") and "AffectedSupport" not in n
                 or n.startswith("sub_AllAffected")]) >= 20
