@@ -194,14 +194,21 @@ def test_segment_isinis_m_and_isinmm_gpu(max_len):
     from tdtdecomposition_gb300 import trusstensor as tt
     rng = np.random.default_rng(max_len)
     n = 3000 if max_len < 100 else 300
-    a, ap = _sorted_rows(rng, n, max_len, 2 * max_len + 5, 0.1)
-    b, bp = _sorted_rows(rng, n, max_len, 2 * max_len + 5, 0.1)
-    for ora, op in ((R.segment_isinis_m, tt.segment_isinis_m), (R.segment_isinmm, tt.segment_isinmm)):
+    # segment_isinis_m takes (a, a_ptr, b, b_ptr) and passes over -1 holes
+    # anywhere; segment_isinmm takes (u, v, u_ptr, v_ptr) and sorted rows
+    for ora, op, order, holes in ((R.segment_isinis_m, tt.segment_isinis_m, (0, 1, 2, 3), 0.1),
+                                  (R.segment_isinmm, tt.segment_isinmm, (0, 2, 1, 3), 0.0)):
+        a, ap = _sorted_rows(rng, n, max_len, 2 * max_len + 5, holes)
+        b, bp = _sorted_rows(rng, n, max_len, 2 * max_len + 5, holes)
+        if holes == 0.0:     # sorted rows that may hold -1 (and other negatives)
+            a -= 3
+            b -= 3
+        args = [(a, ap, b, bp)[i] for i in order]
         m1, m2 = np.zeros(len(a), np.uint8), np.zeros(len(b), np.uint8)
-        ora(a, ap, b, bp, m1, m2)
+        ora(*args, m1, m2)
         g1 = torch.zeros(len(a), dtype=torch.bool, device="cuda")
         g2 = torch.zeros(len(b), dtype=torch.bool, device="cuda")
-        op(_cu(a), _cu(ap), _cu(b), _cu(bp), g1, g2)
+        op(*[_cu(x) for x in args], g1, g2)
         assert np.array_equal(_host(g1), m1) and np.array_equal(_host(g2), m2)
 
 
