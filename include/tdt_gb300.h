@@ -202,8 +202,10 @@ int tdt_sub_affected_support_tile(const int32_t *sub_rows, const int32_t *sub_co
 
 /* Research-variant operators (the reference's `tensor_original` and
  * `undirected` drivers; none is on the `--cuda` flow).  Row-pointer arrays are
- * int32, as the reference's ops read them; every list is sorted ascending
- * without repeated keys (the reference's merge walk relies on it).
+ * int32, as the reference's ops read them.  Two lists pair up exactly as the
+ * reference's two-pointer merge pairs them, whatever their order: strictly
+ * increasing lists take a shared-memory hash path, any others a one-lane
+ * merge walk.
  *
  * segment_isinis_m (myhpu_extension.cpp:255-265; kernel.cu:687-737): for each
  * row r < num_rows, the positions of the values rows r of a and b share, -1

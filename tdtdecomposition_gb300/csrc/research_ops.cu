@@ -22,12 +22,16 @@
 // (the wrappers pass the level + 1 as l, myhpu_extension.cpp:330 etc.).
 // Tiled forms split every list into n_cut column tiles (ptr[v * n_cut + k]).
 //
-// Here one warp takes one (edge, tile): the shorter list goes into a per-warp
-// shared-memory hash (vertex -> position), the longer is streamed and probed.
-// Decrements are exact atomics, so the outcome (supports, n_mark) does not
-// depend on the order.  Input contract (the reference's merge walk relies on
-// it): every list sorted ascending without repeated keys.  List positions and
-// edge ids are bounds-checked; an out-of-range id takes part in no triangle.
+// Every operator here pairs two lists the way the reference's two-pointer
+// merge does.  One warp takes one pair (edge x tile, or row).  It first checks
+// that both lists are strictly increasing (isinis_m: ignoring its -1 holes,
+// with every other value >= 0).  For such lists the merge pairs exactly the
+// equal values, so the warp hashes the shorter list into shared memory
+// (value -> position) and streams the longer one against it.  Otherwise one
+// lane runs the reference's merge walk itself, so the outcome is the
+// reference's on any input.  Decrements are exact atomics: supports and n_mark
+// do not depend on thread order.  List positions and edge ids are
+// bounds-checked; an out-of-range id takes part in no triangle.
 #include "common.cuh"
 
 namespace tdt {
@@ -42,6 +46,118 @@ constexpr int32_t kREmpty = INT32_MIN;
 
 __device__ __forceinline__ unsigned rhash(int32_t k) { return ((uint32_t)k * 0x9E3779B1u) >> 24; }
 
+// ------------------------------------------------------------------ list pairing
+// A list source S gives key(i) for a position i of its array.
+
+// True on every lane when [b, e) of s is strictly increasing (skip_neg1: the
+// -1 entries are left out and every other entry must be >= 0) and holds no
+// INT32_MIN.  Called by all 32 lanes.
+template <class S>
+__device__ bool warp_increasing(const S& s, int64_t b, int64_t e, bool skip_neg1, unsigned lane) {
+    bool ok = true, has_prev = false;
+    int32_t prev = 0;
+    for (int64_t c = b; c < e; c += kWarp) {
+        const int64_t i = c + lane;
+        const bool valid = i < e;
+        const int32_t k = valid ? s.key(i) : 0;
+        if (valid && (k == kREmpty || (skip_neg1 && k < -1))) ok = false;
+        const bool real = valid && !(skip_neg1 && k == -1);
+        const unsigned rm = __ballot_sync(kFull, real);
+        const unsigned below = rm & lanemask_lt();
+        const int32_t pk = __shfl_sync(kFull, k, below ? 31 - __clz(below) : 0);
+        if (real) {
+            if (below) {
+                if (!(pk < k)) ok = false;
+            } else if (has_prev && !(prev < k)) {
+                ok = false;
+            }
+        }
+        if (rm) {
+            prev = __shfl_sync(kFull, k, 31 - __clz(rm));
+            has_prev = true;
+        }
+    }
+    return __all_sync(kFull, ok);
+}
+
+// Hash pairing of two strictly increasing lists: on_match(short_pos, long_pos)
+// for every value both hold (skip_neg1: -1 excepted).  Called by all lanes.
+template <class SS, class SL, class F>
+__device__ void warp_hash_pairs(const SS& S, int64_t sb, int64_t se, const SL& L, int64_t lb, int64_t le,
+                                bool skip_neg1, int32_t* hkey, int32_t* hpos, unsigned lane, F&& on_match) {
+    for (int64_t c = sb; c < se; c += kRChunk) {
+        const int64_t ce = c + kRChunk < se ? c + kRChunk : se;
+        for (int i = lane; i < kRSlots; i += kWarp) hkey[i] = kREmpty;
+        __syncwarp();
+        for (int64_t i = c + lane; i < ce; i += kWarp) {
+            const int32_t key = S.key(i);
+            if (skip_neg1 && key == -1) continue;
+            unsigned h = rhash(key);
+            for (int probe = 0; probe < kRSlots; probe++) {
+                if (atomicCAS(&hkey[h], kREmpty, key) == kREmpty) {
+                    hpos[h] = (int32_t)(i - c);
+                    break;
+                }
+                h = (h + 1) & (kRSlots - 1);
+            }
+        }
+        __syncwarp();
+        for (int64_t i = lb + lane; i < le; i += kWarp) {
+            const int32_t key = L.key(i);
+            if (skip_neg1 && key == -1) continue;
+            unsigned h = rhash(key);
+            for (int probe = 0; probe < kRSlots; probe++) {
+                const int32_t kk = hkey[h];
+                if (kk == kREmpty) break;
+                if (kk == key) {
+                    on_match(c + hpos[h], i);
+                    break;
+                }
+                h = (h + 1) & (kRSlots - 1);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// The reference's two-pointer walk (e.g. kernel.cu:822-857), run by one lane.
+template <class SA, class SB, class F>
+__device__ void lane_merge(const SA& A, int64_t i, int64_t ie, const SB& B, int64_t j, int64_t je, bool skip_neg1,
+                           F&& on_match) {
+    while (i < ie && j < je) {
+        const int32_t x = A.key(i), y = B.key(j);
+        if (x == y && !(skip_neg1 && x == -1)) {
+            on_match(i, j);
+            i++;
+            j++;
+        } else if (x < y) {
+            i++;
+        } else {
+            j++;
+        }
+    }
+}
+
+// Pair list A [ab, ae) with list B [bb, be): on_match(posA, posB) for the
+// pairs the reference's merge would match.  Called by all lanes.
+template <class SA, class SB, class F>
+__device__ void warp_pairs(const SA& A, int64_t ab, int64_t ae, const SB& B, int64_t bb, int64_t be, bool skip_neg1,
+                           int32_t* hkey, int32_t* hpos, unsigned lane, F&& on_match) {
+    if (ae <= ab || be <= bb) return;
+    if (warp_increasing(A, ab, ae, skip_neg1, lane) && warp_increasing(B, bb, be, skip_neg1, lane)) {
+        if (ae - ab <= be - bb) {
+            warp_hash_pairs(A, ab, ae, B, bb, be, skip_neg1, hkey, hpos, lane, on_match);
+        } else {
+            warp_hash_pairs(B, bb, be, A, ab, ae, skip_neg1, hkey, hpos, lane,
+                            [&](int64_t pb, int64_t pa) { on_match(pa, pb); });
+        }
+    } else {
+        if (lane == 0) lane_merge(A, ab, ae, B, bb, be, skip_neg1, on_match);
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ peel updates
 enum ListKind { kOut = 0, kIn = 1, kUnd = 2 };
 enum Variant { kVarUnd = 0, kVarOO = 1, kVarII = 2, kVarOI = 3 };
 
@@ -68,39 +184,36 @@ struct PeelOpArgs {
     int32_t n_cut;
 };
 
-// A list of (key = third vertex, edge id) pairs: positions [b, e).
-struct ListView {
-    int kind;
-    int64_t b, e;
-    __device__ __forceinline__ void key_eid(const PeelOpArgs& A, int64_t i, int32_t& key, int32_t& eid) const {
-        if (kind == kOut) {
-            eid = (int32_t)i;
-            key = __ldg(A.columns + i);
-        } else if (kind == kIn) {
-            eid = __ldg(A.r_edges + i);
-            key = (eid >= 0 && eid < A.E) ? __ldg(A.rows + eid) : kREmpty;
-        } else {
-            eid = __ldg(A.edges_id_nbr + i);
-            key = __ldg(A.columns_g + i);
-        }
+// Third-vertex keys and edge ids of one list kind.
+template <int K>
+struct EdgeList {
+    const PeelOpArgs* A;
+    __device__ __forceinline__ int32_t id(int64_t i) const {
+        if (K == kOut) return (int32_t)i;
+        if (K == kIn) return __ldg(A->r_edges + i);
+        return __ldg(A->edges_id_nbr + i);
+    }
+    __device__ __forceinline__ int32_t key(int64_t i) const {
+        if (K == kOut) return __ldg(A->columns + i);
+        if (K == kUnd) return __ldg(A->columns_g + i);
+        const int32_t x = __ldg(A->r_edges + i);
+        return (x >= 0 && x < A->E) ? __ldg(A->rows + x) : kREmpty;
     }
 };
 
-__device__ __forceinline__ ListView make_list(const PeelOpArgs& A, int kind, int32_t v, int k) {
-    ListView L;
-    L.kind = kind;
-    L.b = L.e = 0;
-    const int32_t* ptr = kind == kIn ? A.re_ptr : A.row_ptr;
-    const int64_t plen = kind == kIn ? A.re_ptr_len : A.row_ptr_len;
-    const int64_t cap = kind == kOut ? A.E : (kind == kIn ? A.r_len : A.g_len);
+template <int K>
+__device__ __forceinline__ void list_range(const PeelOpArgs& A, int32_t v, int k, int64_t& b, int64_t& e) {
+    const int32_t* ptr = K == kIn ? A.re_ptr : A.row_ptr;
+    const int64_t plen = K == kIn ? A.re_ptr_len : A.row_ptr_len;
+    const int64_t cap = K == kOut ? A.E : (K == kIn ? A.r_len : A.g_len);
     const int64_t j = (int64_t)v * A.n_cut + k;
-    if (v < 0 || j + 1 >= plen) return L;
-    int64_t b = __ldg(ptr + j), e = __ldg(ptr + j + 1);
-    b = b < 0 ? 0 : (b > cap ? cap : b);
-    e = e < b ? b : (e > cap ? cap : e);
-    L.b = b;
-    L.e = e;
-    return L;
+    b = e = 0;
+    if (v < 0 || j + 1 >= plen) return;
+    int64_t x = __ldg(ptr + j), y = __ldg(ptr + j + 1);
+    x = x < 0 ? 0 : (x > cap ? cap : x);
+    y = y < x ? x : (y > cap ? cap : y);
+    b = x;
+    e = y;
 }
 
 __device__ __forceinline__ void dec_mark(const PeelOpArgs& A, int32_t x) {
@@ -124,14 +237,14 @@ __device__ __forceinline__ void on_shared(const PeelOpArgs& A, int32_t e, int32_
 
 template <int V>
 __global__ void __launch_bounds__(kRBlock) peel_op_kernel(PeelOpArgs A) {
+    constexpr int KA = V == kVarII ? kIn : (V == kVarUnd ? kUnd : kOut);
+    constexpr int KB = V == kVarOO ? kOut : (V == kVarUnd ? kUnd : kIn);
     __shared__ int32_t s_key[kRWarps][kRSlots];
-    __shared__ int32_t s_eid[kRWarps][kRSlots];
+    __shared__ int32_t s_pos[kRWarps][kRSlots];
     const int wib = threadIdx.x / kWarp;
     const unsigned lane = lane_id();
-    int32_t* hkey = s_key[wib];
-    int32_t* heid = s_eid[wib];
-    const int ka = V == kVarII ? kIn : (V == kVarUnd ? kUnd : kOut);
-    const int kb = V == kVarOO ? kOut : (V == kVarUnd ? kUnd : kIn);
+    const EdgeList<KA> LA{&A};
+    const EdgeList<KB> LB{&A};
     const int64_t units = A.n_curr * A.n_cut;
     const int64_t nw = (int64_t)gridDim.x * kRWarps;
     for (int64_t w = (int64_t)blockIdx.x * kRWarps + wib; w < units; w += nw) {
@@ -139,55 +252,21 @@ __global__ void __launch_bounds__(kRBlock) peel_op_kernel(PeelOpArgs A) {
         const int k = (int)(w % A.n_cut);
         const int32_t e = __ldg(A.e_curr + j);
         if (e < 0 || e >= A.E) continue;
-        const int32_t u = __ldg(A.rows + e), v = __ldg(A.columns + e);
-        const ListView La = make_list(A, ka, u, k), Lb = make_list(A, kb, v, k);
-        if (La.e <= La.b || Lb.e <= Lb.b) continue;
-        const bool a_short = La.e - La.b <= Lb.e - Lb.b;
-        const ListView& S = a_short ? La : Lb;
-        const ListView& Lg = a_short ? Lb : La;
-        for (int64_t c = S.b; c < S.e; c += kRChunk) {
-            const int64_t ce = c + kRChunk < S.e ? c + kRChunk : S.e;
-            for (int i = lane; i < kRSlots; i += kWarp) hkey[i] = kREmpty;
-            __syncwarp();
-            for (int64_t i = c + lane; i < ce; i += kWarp) {
-                int32_t key, eid;
-                S.key_eid(A, i, key, eid);
-                if (key == kREmpty) continue;
-                unsigned h = rhash(key);
-                for (int probe = 0; probe < kRSlots; probe++) {
-                    if (atomicCAS(&hkey[h], kREmpty, key) == kREmpty) {
-                        heid[h] = eid;
-                        break;
-                    }
-                    h = (h + 1) & (kRSlots - 1);
-                }
-            }
-            __syncwarp();
-            for (int64_t i = Lg.b + lane; i < Lg.e; i += kWarp) {
-                int32_t key, eid;
-                Lg.key_eid(A, i, key, eid);
-                if (key == kREmpty) continue;
-                unsigned h = rhash(key);
-                for (int probe = 0; probe < kRSlots; probe++) {
-                    const int32_t kk = hkey[h];
-                    if (kk == kREmpty) break;
-                    if (kk == key) {
-                        const int32_t se = heid[h];
-                        if (a_short) on_shared<V>(A, e, se, eid); else on_shared<V>(A, e, eid, se);
-                        break;
-                    }
-                    h = (h + 1) & (kRSlots - 1);
-                }
-            }
-            __syncwarp();
-        }
+        int64_t ab, ae, bb, be;
+        list_range<KA>(A, __ldg(A.rows + e), k, ab, ae);
+        list_range<KB>(A, __ldg(A.columns + e), k, bb, be);
+        warp_pairs(LA, ab, ae, LB, bb, be, false, s_key[wib], s_pos[wib], lane,
+                   [&](int64_t pa, int64_t pb) { on_shared<V>(A, e, LA.id(pa), LB.id(pb)); });
     }
 }
 
-// segment_isinis_m / segment_isinmm: row r of a and row r of b (sorted),
-// flag the positions of shared values.  skip_neg1: the -1 sentinels of
-// isinis_m never match (they are passed over by the reference's merge wherever
-// they stand, so removing them first gives the same pairs).
+// ------------------------------------------------------------------ row-wise match masks
+struct PlainList {
+    const int32_t* v;
+    __device__ __forceinline__ int32_t key(int64_t i) const { return __ldg(v + i); }
+};
+
+// segment_isinis_m (skip_neg1) / segment_isinmm: row r of a against row r of b.
 __global__ void __launch_bounds__(kRBlock) isin_mask_kernel(const int32_t* a_cols, int64_t a_len, const int32_t* a_rp,
                                                             const int32_t* b_cols, int64_t b_len, const int32_t* b_rp,
                                                             int64_t rows, uint8_t* m1, uint8_t* m2,
@@ -196,8 +275,7 @@ __global__ void __launch_bounds__(kRBlock) isin_mask_kernel(const int32_t* a_col
     __shared__ int32_t s_pos[kRWarps][kRSlots];
     const int wib = threadIdx.x / kWarp;
     const unsigned lane = lane_id();
-    int32_t* hkey = s_key[wib];
-    int32_t* hpos = s_pos[wib];
+    const PlainList A{a_cols}, B{b_cols};
     const int64_t nw = (int64_t)gridDim.x * kRWarps;
     for (int64_t r = (int64_t)blockIdx.x * kRWarps + wib; r < rows; r += nw) {
         int64_t ab = __ldg(a_rp + r), ae = __ldg(a_rp + r + 1), bb = __ldg(b_rp + r), be = __ldg(b_rp + r + 1);
@@ -205,48 +283,11 @@ __global__ void __launch_bounds__(kRBlock) isin_mask_kernel(const int32_t* a_col
         ae = ae < ab ? ab : (ae > a_len ? a_len : ae);
         bb = bb < 0 ? 0 : (bb > b_len ? b_len : bb);
         be = be < bb ? bb : (be > b_len ? b_len : be);
-        if (ae <= ab || be <= bb) continue;
-        const bool a_short = ae - ab <= be - bb;
-        const int32_t* sc = a_short ? a_cols : b_cols;
-        const int32_t* lc = a_short ? b_cols : a_cols;
-        uint8_t* sm = a_short ? m1 : m2;
-        uint8_t* lm = a_short ? m2 : m1;
-        const int64_t s0 = a_short ? ab : bb, s1 = a_short ? ae : be;
-        const int64_t l0 = a_short ? bb : ab, l1 = a_short ? be : ae;
-        for (int64_t c = s0; c < s1; c += kRChunk) {
-            const int64_t ce = c + kRChunk < s1 ? c + kRChunk : s1;
-            for (int i = lane; i < kRSlots; i += kWarp) hkey[i] = kREmpty;
-            __syncwarp();
-            for (int64_t i = c + lane; i < ce; i += kWarp) {
-                const int32_t key = __ldg(sc + i);
-                if (key == kREmpty || (skip_neg1 && key == -1)) continue;
-                unsigned h = rhash(key);
-                for (int probe = 0; probe < kRSlots; probe++) {
-                    if (atomicCAS(&hkey[h], kREmpty, key) == kREmpty) {
-                        hpos[h] = (int32_t)(i - c);
-                        break;
-                    }
-                    h = (h + 1) & (kRSlots - 1);
-                }
-            }
-            __syncwarp();
-            for (int64_t i = l0 + lane; i < l1; i += kWarp) {
-                const int32_t key = __ldg(lc + i);
-                if (key == kREmpty || (skip_neg1 && key == -1)) continue;
-                unsigned h = rhash(key);
-                for (int probe = 0; probe < kRSlots; probe++) {
-                    const int32_t kk = hkey[h];
-                    if (kk == kREmpty) break;
-                    if (kk == key) {
-                        sm[c + hpos[h]] = 1;
-                        lm[i] = 1;
-                        break;
-                    }
-                    h = (h + 1) & (kRSlots - 1);
-                }
-            }
-            __syncwarp();
-        }
+        warp_pairs(A, ab, ae, B, bb, be, skip_neg1 != 0, s_key[wib], s_pos[wib], lane,
+                   [&](int64_t pa, int64_t pb) {
+                       m1[pa] = 1;
+                       m2[pb] = 1;
+                   });
     }
 }
 

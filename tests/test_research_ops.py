@@ -188,27 +188,45 @@ def _sorted_rows(rng, n_rows, max_len, universe, holes):
     return cols, ptr
 
 
+def _messy(rng, cols, ptr, shape):
+    """Rows the reference's merge still walks, but not strictly increasing."""
+    cols = cols.copy()
+    if shape == "holes":
+        cols[rng.random(cols.shape[0]) < 0.1] = -1
+    elif shape == "shuffled":
+        for r in range(len(ptr) - 1):
+            if rng.random() < 0.3:
+                rng.shuffle(cols[ptr[r]:ptr[r + 1]])
+    elif shape == "dups":
+        d = rng.random(cols.shape[0]) < 0.2
+        d[ptr[:-1][ptr[:-1] < cols.shape[0]]] = False
+        cols[d] = np.roll(cols, 1)[d]
+    return cols
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape", ["sorted", "holes", "shuffled", "dups"])
 @pytest.mark.parametrize("max_len", [6, 90, 700])
-def test_segment_isinis_m_and_isinmm_gpu(max_len):
+def test_segment_isinis_m_and_isinmm_gpu(max_len, shape):
+    """Both row-wise match ops give the reference's merge-walk marks: sorted
+    rows (hash path) and rows with -1 holes, shuffled rows and repeated values
+    (one-lane merge, or the hash path where the holes are isinis_m's)."""
     from tdtdecomposition_gb300 import trusstensor as tt
     rng = np.random.default_rng(max_len)
     n = 3000 if max_len < 100 else 300
-    # segment_isinis_m takes (a, a_ptr, b, b_ptr) and passes over -1 holes
-    # anywhere; segment_isinmm takes (u, v, u_ptr, v_ptr) and sorted rows
-    for ora, op, order, holes in ((R.segment_isinis_m, tt.segment_isinis_m, (0, 1, 2, 3), 0.1),
-                                  (R.segment_isinmm, tt.segment_isinmm, (0, 2, 1, 3), 0.0)):
-        a, ap = _sorted_rows(rng, n, max_len, 2 * max_len + 5, holes)
-        b, bp = _sorted_rows(rng, n, max_len, 2 * max_len + 5, holes)
-        if holes == 0.0:     # sorted rows that may hold -1 (and other negatives)
-            a -= 3
-            b -= 3
+    # segment_isinis_m takes (a, a_ptr, b, b_ptr), segment_isinmm (u, v, u_ptr, v_ptr)
+    for ora, op, order in ((R.segment_isinis_m, tt.segment_isinis_m, (0, 1, 2, 3)),
+                           (R.segment_isinmm, tt.segment_isinmm, (0, 2, 1, 3))):
+        a, ap = _sorted_rows(rng, n, max_len, 2 * max_len + 5, 0.0)
+        b, bp = _sorted_rows(rng, n, max_len, 2 * max_len + 5, 0.0)
+        a, b = _messy(rng, a - 3, ap, shape), _messy(rng, b - 3, bp, shape)
         args = [(a, ap, b, bp)[i] for i in order]
         m1, m2 = np.zeros(len(a), np.uint8), np.zeros(len(b), np.uint8)
         ora(*args, m1, m2)
         g1 = torch.zeros(len(a), dtype=torch.bool, device="cuda")
         g2 = torch.zeros(len(b), dtype=torch.bool, device="cuda")
         op(*[_cu(x) for x in args], g1, g2)
+        assert m1.any()
         assert np.array_equal(_host(g1), m1) and np.array_equal(_host(g2), m2)
 
 
@@ -270,6 +288,51 @@ def test_peel_operators_gpu(variant, n_cut):
         lists = {"oo": (_cu(rp_t),), "ii": (_cu(r_e), _cu(re_p)), "oi": (_cu(rp_t), _cu(r_e), _cu(re_p))}[variant]
         fn = getattr(tt, "peeling_direct_%s%s" % ("tile_" if n_cut > 1 else "", variant))
     fn(*common, *lists, *tail, *((n_cut,) if n_cut > 1 else ()))
+    assert (want_s != sup).any()
+    assert np.array_equal(_host(gs), want_s)
+    assert np.array_equal(_host(gm), want_m)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["oo", "ii", "undirect"])
+def test_peel_operators_on_unsorted_lists_gpu(variant):
+    """Lists out of order (shuffled in-lists, shuffled symmetric adjacency,
+    shuffled out-lists): the one-lane merge path gives the reference's
+    decrements and marks."""
+    from tdtdecomposition_gb300 import trusstensor as tt
+    rows, cols, rp, nv, sup, e_mask, in_curr, e_curr, l = _peel_case(5, 11, 1)
+    rng = np.random.default_rng(1)
+    E = len(cols)
+    want_s, want_m = sup.copy(), np.zeros(E, np.uint8)
+    gs, gm = _cu(sup), torch.zeros(E, dtype=torch.bool, device="cuda")
+    if variant == "undirect":
+        dp, cg, nbr, pg = R.preprocess_undirect(rows, cols, rp, nv, 1, 1)
+        perm = np.arange(len(cg))
+        for v in range(nv):
+            if rng.random() < 0.3:
+                rng.shuffle(perm[pg[v]:pg[v + 1]])
+        cg, nbr = cg[perm], nbr[perm]
+        R.peel_op(R.UNDIRECT, e_curr, rows, cols, want_s, e_mask, want_m, in_curr, l, 1, row_ptr=pg, columns_g=cg,
+                  edges_id_nbr=nbr)
+        tt.peeling_undirect(_cu(e_curr), _cu(rows), _cu(cols), _cu(cg), _cu(pg), _cu(nbr), gs,
+                            _cu(e_mask, torch.bool), gm, _cu(in_curr, torch.bool), l)
+    else:
+        rp_t, r_e, re_p = R.preprocess_direct(rows, cols, rp, nv, 1)
+        if variant == "ii":
+            for v in range(nv):
+                if rng.random() < 0.3:
+                    rng.shuffle(r_e[re_p[v]:re_p[v + 1]])
+            R.peel_op(R.II, e_curr, rows, cols, want_s, e_mask, want_m, in_curr, l, 1, r_edges=r_e, re_ptr=re_p)
+            tt.peeling_direct_ii(_cu(e_curr), _cu(rows), _cu(cols), _cu(r_e), _cu(re_p), gs,
+                                 _cu(e_mask, torch.bool), gm, _cu(in_curr, torch.bool), l)
+        else:
+            cols = cols.copy()
+            for v in range(nv):
+                if rng.random() < 0.3:
+                    rng.shuffle(cols[rp_t[v]:rp_t[v + 1]])
+            R.peel_op(R.OO, e_curr, rows, cols, want_s, e_mask, want_m, in_curr, l, 1, row_ptr=rp_t)
+            tt.peeling_direct_oo(_cu(e_curr), _cu(rows), _cu(cols), _cu(rp_t), gs, _cu(e_mask, torch.bool), gm,
+                                 _cu(in_curr, torch.bool), l)
     assert (want_s != sup).any()
     assert np.array_equal(_host(gs), want_s)
     assert np.array_equal(_host(gm), want_m)
