@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--skewed", action="store_true",
                     help="also run the skewed Chung-Lu graph (n=2^25): triangle count, decomposition, k-truss")
     ap.add_argument("--skewed-log2n", type=int, default=25)
+    ap.add_argument("--fusion", action="store_true",
+                    help="add the fusion-experiment line (unfused vs fused support count)")
+    ap.add_argument("--fusion-scale", type=int, default=20)
     return ap.parse_args()
 
 
@@ -314,6 +317,50 @@ def bench_skewed(dev, log2n=25):
             "ktruss": kt, "ktruss_equals_truss_ge_k": True}
 
 
+# ---------------------------------------------------------------- fusion ablation
+def bench_fusion(dev, scale=20, reps=3):
+    """The fusion experiment (fusionexperiental.py:24-46, EXP3 "ComputeSup"
+    vs "ComputeSup+") on R-MAT scale `scale`, edge factor 16, seed 1: the
+    unfused support count (gather both out-lists of every edge,
+    segment_isinmm, segment_add and two unique/count passes) against the
+    fused segment_isin2 drop-in op.  Both give the same supports (checked).
+    Median of `reps` timed runs after one warm-up each."""
+    import torch
+    from tdtdecomposition_gb300 import flow, generators as G
+    from tdtdecomposition_gb300.preprocess import preprocess_edges
+    src, dst = G.rmat_edges_device(scale, 16 << scale, seed=1, device=dev)
+    g, _ = preprocess_edges(src, dst)
+    del src, dst
+    rp32 = g.row_ptr.to(torch.int32)
+    deg = (g.row_ptr[1:] - g.row_ptr[:-1])
+    gathered = int(deg[g.rows.long()].sum()) + int(deg[g.columns.long()].sum())
+    free, _ = torch.cuda.mem_get_info(dev)
+    if gathered * 24 > 0.6 * free:
+        return {"workload": "R-MAT scale %d, edge factor 16, seed 1" % scale,
+                "skipped": "the unfused count gathers %d list entries; too large for free memory" % gathered}
+
+    def timed(fn):
+        fn()
+        out, ms = None, []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            out = fn()
+            b.record()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return out, sorted(ms)[len(ms) // 2]
+
+    fused, t_fused = timed(lambda: flow.support_computing(g.rows, g.columns, rp32, 1))
+    unfused, t_unfused = timed(lambda: flow.support_computing_before(g.rows, g.columns, rp32, 1))
+    if not torch.equal(fused, unfused):
+        raise SystemExit("unfused and fused support counts differ")
+    return {"workload": "R-MAT scale %d, edge factor 16, seed 1" % scale, "V": g.num_vertices, "E": g.num_edges,
+            "gathered_list_entries": gathered, "triangles": int(fused.to(torch.int64).sum()) // 3,
+            "compute_sup_ms": t_unfused, "compute_sup_plus_ms": t_fused, "fused_speedup": t_unfused / t_fused}
+
+
 # ---------------------------------------------------------------- served workload
 def bench_served(dev, n_requests=48, rates=(8.0, 32.0, 128.0)):
     """Poisson request streams (the same 48 seeded requests replayed at each
@@ -565,6 +612,8 @@ def main_ours(args):
         line["served"] = bench_served(dev)
     if args.skewed:
         line["skewed"] = bench_skewed(dev, args.skewed_log2n)
+    if args.fusion:
+        line["fusion"] = bench_fusion(dev, args.fusion_scale)
     if not args.no_cpu_baseline:
         sc = cpu_sample_scale(args, 1)
         Ec, Vc, times, threads = cpu_decompose_sample(sc, 1)

@@ -61,12 +61,90 @@ def _batched_csr_selection(starts, ends):
     return starts.to(torch.int64)[seg] + (torch.arange(total, device=starts.device) - first[seg])
 
 
-def k_truss(graph, n_cut, num_v, cpu_flow=False, compact_threshold=1000000):
+def _csr_selection_ptr(starts, ends):
+    """batched_csr_selection_opt (helper.py:87-101): flat positions of all
+    [starts[i], ends[i]) ranges and their int32 offsets."""
+    sizes = (ends - starts).to(torch.int64).clamp_(min=0)
+    ptr = torch.zeros(sizes.shape[0] + 1, dtype=torch.int32, device=starts.device)
+    ptr[1:] = torch.cumsum(sizes, 0).to(torch.int32)
+    return _batched_csr_selection(starts, starts + sizes), ptr
+
+
+def _rows_of(row_ptr, v, n_cut):
+    """Whole-row ranges of vertices v in a (tiled) row_ptr."""
+    rp = row_ptr.to(torch.int64)
+    v = v.to(torch.int64)
+    return rp[v * n_cut], rp[v * n_cut + n_cut]
+
+
+# ------------------------------------------------------------------ fusion ablation ("before" ops)
+def support_computing_before(sub_rows, sub_columns, tiling_row_ptr, n_cut):
+    """fusionexperiental.py:24-46: the unfused support count the reference
+    times as "ComputeSup" against segment_isin2 ("ComputeSup+").  Every edge
+    (u, v) gathers N+(u) and N+(v), segment_isinmm marks their common
+    neighbours, and three separate passes count the triangles of (u, v),
+    (u, w) and (v, w).  The reference calls it with n_cut = 1 and indexes
+    row_ptr[u], row_ptr[u + 1]; whole rows (row_ptr[u * n_cut] ..
+    row_ptr[u * n_cut + n_cut]) are the same there and stay right for tiled
+    offsets.  Same result as support_computing."""
+    E = sub_columns.shape[0]
+    support = torch.zeros(E, dtype=torch.int32, device=sub_columns.device)
+    I_u, uptr = _csr_selection_ptr(*_rows_of(tiling_row_ptr, sub_rows, n_cut))
+    I_v, vptr = _csr_selection_ptr(*_rows_of(tiling_row_ptr, sub_columns, n_cut))
+    M_u = torch.zeros(I_u.shape[0], dtype=torch.bool, device=support.device)
+    M_v = torch.zeros(I_v.shape[0], dtype=torch.bool, device=support.device)
+    tt.segment_isinmm(sub_columns[I_u], sub_columns[I_v], uptr, vptr, M_u, M_v)
+    tt.segment_add(M_u.int(), uptr, support)
+    I_uw, ct = torch.unique(I_u[M_u], return_counts=True)
+    support[I_uw] += ct.to(torch.int32)
+    I_vw, ct = torch.unique(I_v[M_v], return_counts=True)
+    support[I_vw] += ct.to(torch.int32)
+    return support
+
+
+def all_affect_support_not_before(e_affect, graph, n_cut, mask, l, n_mark, support):
+    """fusionexperiental.py:48-67: the unfused peel update (the reference
+    defines it next to its timed support phase and never reaches it).  For
+    each affected edge (u, v), segment_isinmm pairs N+(u) with N+(v); a
+    triangle whose (u, w) column is live and whose three edges are not all in
+    `mask` is destroyed: all three edges lose one, and the touched edges in
+    `mask` that end at or below l are set in n_mark.  Affected edges whose
+    column is already -1 (peeled) carry no triangle here; the reference would
+    index row_ptr[-1] for them.  Same n_mark as all_affect_support_not."""
+    e_affect = e_affect.to(torch.int64)
+    e_affect = e_affect[graph.columns[e_affect] >= 0]
+    U = graph.rows[e_affect]
+    V = graph.columns[e_affect]
+    I_u, uptr = _csr_selection_ptr(*_rows_of(graph.row_ptr, U, n_cut))
+    I_v, vptr = _csr_selection_ptr(*_rows_of(graph.row_ptr, V, n_cut))
+    M_u = torch.zeros(I_u.shape[0], dtype=torch.bool, device=support.device)
+    M_v = torch.zeros(I_v.shape[0], dtype=torch.bool, device=support.device)
+    tt.segment_isinmm(graph.columns[I_u], graph.columns[I_v], uptr, vptr, M_u, M_v)
+    sizes = torch.zeros(e_affect.shape[0], dtype=torch.int32, device=support.device)
+    tt.segment_add(M_u.int(), uptr, sizes)
+    I_uv = torch.repeat_interleave(e_affect, sizes.to(torch.int64))
+    I_uw = I_u[M_u]
+    I_vw = I_v[M_v]
+    M_tri = (graph.columns[I_uw] > 0) & (~(mask[I_uv] & mask[I_uw] & mask[I_vw]))
+    I_e = torch.cat([I_uv[M_tri], I_uw[M_tri], I_vw[M_tri]])
+    I_ue, counts = torch.unique(I_e, return_counts=True)
+    support[I_ue] -= counts.to(torch.int32)
+    n_mark[I_ue] = mask[I_ue] & (support[I_ue] <= l)
+    return n_mark, support
+
+
+def k_truss(graph, n_cut, num_v, cpu_flow=False, compact_threshold=1000000, fused=True):
     """singlegpu_truss.py:67-158 (cpu_flow=False, peel update = *_not) or
     test/truss_setup.py:61-154 (cpu_flow=True, peel update = sub_AllAffectedSupport*).
+    fused=False runs the fusion experiment's unfused operators instead
+    (support_computing_before, all_affect_support_not_before;
+    fusionexperiental.py:24-67) with the same results.
     Mutates graph like the reference.  Returns (kmax, e_truss, ptr_truss)."""
     dev = graph.device
-    support = support_computing(graph.rows, graph.columns, graph.row_ptr, n_cut)
+    if fused:
+        support = support_computing(graph.rows, graph.columns, graph.row_ptr, n_cut)
+    else:
+        support = support_computing_before(graph.rows, graph.columns, graph.row_ptr, n_cut)
     e_truss = torch.zeros(0, dtype=torch.int32, device=dev)
     ptr_truss = [0]
     l = 1
@@ -99,8 +177,10 @@ def k_truss(graph, n_cut, num_v, cpu_flow=False, compact_threshold=1000000):
         n_mark = torch.zeros(graph.columns.shape[0], dtype=torch.bool, device=dev)
         if cpu_flow:
             all_affect_support(e_affect, graph, n_cut, e_mask, l, n_mark, support)
-        else:
+        elif fused:
             all_affect_support_not(e_affect, graph, n_cut, e_mask, l, n_mark, support)
+        else:
+            all_affect_support_not_before(e_affect, graph, n_cut, e_mask, l, n_mark, support)
         graph.columns[e_curr] = -1
         peeled += e_curr.shape[0]
         if peeled > compact_threshold:

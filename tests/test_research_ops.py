@@ -385,3 +385,56 @@ def test_flow_undirected_direct_matches_decomposition_gpu():
     res = T.truss_decompose(g)
     assert k == res.kmax
     assert np.array_equal(GD.truss_from_levels(_host(e), _host(p), len(cols)), _host(res.truss))
+
+
+# ------------------------------------------------------------------ fusion ablation ("before" flows)
+def _isinmm_ops():
+    return types.SimpleNamespace(
+        segment_add=lambda c, p, o: O.segment_add(_np(c), _np(p), _np(o)),
+        segment_isinmm=lambda u, v, up, vp, um, vm: R.segment_isinmm(_np(u), _np(v), _np(up), _np(vp), _np(um),
+                                                                     _np(vm)))
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("n_cut,compact", [(1, 1000000), (2, 1000000), (2, 0)])
+def test_unfused_flow_reproduces_reference_peel_order(monkeypatch, name, n_cut, compact):
+    """k_truss(fused=False): support_computing_before and
+    all_affect_support_not_before (fusionexperiental.py:24-67) over the
+    oracle's segment_isinmm / segment_add give the reference's recorded
+    e_truss / ptr_truss exactly."""
+    monkeypatch.setattr(flow, "tt", _isinmm_ops())
+    d = GD.load(name)
+    V = d["ref_vertices"].shape[0]
+    g = CSRCOO(columns=torch.as_tensor(d["ref_cols"], dtype=torch.int32),
+               row_ptr=torch.as_tensor(d["ref_rp_tiled%d" % n_cut], dtype=torch.int32),
+               rows=torch.as_tensor(d["ref_rows"], dtype=torch.int32))
+    sup = flow.support_computing_before(g.rows, g.columns, g.row_ptr, n_cut)
+    assert np.array_equal(sup.numpy(), d["ref_support"])
+    kmax, et, pt = flow.k_truss(g, n_cut, V, compact_threshold=compact, fused=False)
+    assert kmax == int(d["sg_kmax%d" % n_cut])
+    assert np.array_equal(et.numpy(), d["sg_e_truss%d" % n_cut])
+    assert np.array_equal(pt.numpy(), d["sg_ptr_truss%d" % n_cut])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_unfused_flow_gpu(name):
+    d = GD.load(name)
+    V = d["ref_vertices"].shape[0]
+    g = CSRCOO(columns=_cu(d["ref_cols"]), row_ptr=_cu(d["ref_rp_tiled2"]), rows=_cu(d["ref_rows"]))
+    sup = flow.support_computing_before(g.rows, g.columns, g.row_ptr, 2)
+    assert np.array_equal(_host(sup), d["ref_support"])
+    kmax, et, pt = flow.k_truss(g, 2, V, fused=False)
+    assert kmax == int(d["sg_kmax2"])
+    assert np.array_equal(_host(et), d["sg_e_truss2"])
+    assert np.array_equal(pt.numpy(), d["sg_ptr_truss2"])
+
+
+@pytest.mark.gpu
+def test_unfused_support_matches_fused_on_rmat_gpu():
+    s, t = G.rmat_edges(15, 16 << 15, seed=4)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, t], 1))
+    rp32 = _cu(rp)
+    a = flow.support_computing(_cu(rows), _cu(cols), rp32, 1)
+    b = flow.support_computing_before(_cu(rows), _cu(cols), rp32, 1)
+    assert torch.equal(a, b) and int(a.sum()) > 0
