@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--skewed-log2n", type=int, default=25)
     ap.add_argument("--fusion", action="store_true",
                     help="add the fusion-experiment line (unfused vs fused support count)")
-    ap.add_argument("--fusion-scale", type=int, default=20)
+    ap.add_argument("--fusion-scale", type=int, default=18)
     return ap.parse_args()
 
 
@@ -318,7 +318,7 @@ def bench_skewed(dev, log2n=25):
 
 
 # ---------------------------------------------------------------- fusion ablation
-def bench_fusion(dev, scale=20, reps=3):
+def bench_fusion(dev, scale=18, reps=3):
     """The fusion experiment (fusionexperiental.py:24-46, EXP3 "ComputeSup"
     vs "ComputeSup+") on R-MAT scale `scale`, edge factor 16, seed 1: the
     unfused support count (gather both out-lists of every edge,
@@ -356,9 +356,35 @@ def bench_fusion(dev, scale=20, reps=3):
     unfused, t_unfused = timed(lambda: flow.support_computing_before(g.rows, g.columns, rp32, 1))
     if not torch.equal(fused, unfused):
         raise SystemExit("unfused and fused support counts differ")
-    return {"workload": "R-MAT scale %d, edge factor 16, seed 1" % scale, "V": g.num_vertices, "E": g.num_edges,
-            "gathered_list_entries": gathered, "triangles": int(fused.to(torch.int64).sum()) // 3,
-            "compute_sup_ms": t_unfused, "compute_sup_plus_ms": t_fused, "fused_speedup": t_unfused / t_fused}
+    out = {"workload": "R-MAT scale %d, edge factor 16, seed 1" % scale, "V": g.num_vertices, "E": g.num_edges,
+           "gathered_list_entries": gathered, "triangles": int(fused.to(torch.int64).sum()) // 3,
+           "compute_sup_ms": t_unfused, "compute_sup_plus_ms": t_fused, "fused_speedup": t_unfused / t_fused}
+    # the full-decomposition ablation (EXP3.2 columns) on the reference's
+    # host-driven flow (n_cut = 1), and the device-resident path beside it
+    from tdtdecomposition_gb300 import CSRCOO, truss as T
+    abl, want = {}, None
+    for name, fs, fu in (("TDT-origin", False, False), ("+Comp", True, False), ("+Update", False, True),
+                         ("+both", True, True)):
+        h = CSRCOO(columns=g.columns.clone(), row_ptr=rp32.clone(), rows=g.rows.clone())
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        kmax, et, pt = flow.k_truss(h, 1, g.num_vertices, fused_support=fs, fused_update=fu)
+        torch.cuda.synchronize()
+        abl[name] = time.perf_counter() - t
+        if want is None:
+            want = (kmax, et, pt)
+        elif kmax != want[0] or not torch.equal(et, want[1]) or not torch.equal(pt, want[2]):
+            raise SystemExit("ablation variant %s peels differently" % name)
+    res = T.truss_decompose(g)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    res = T.truss_decompose(g)
+    abl["device-resident"] = time.perf_counter() - t
+    if res.kmax != want[0] or not torch.equal(res.e_truss.to(torch.int32), want[1].to(torch.int32)):
+        raise SystemExit("the device-resident decomposition peels differently from the flow")
+    out["decomposition_s"] = abl
+    out["kmax"] = want[0]
+    return out
 
 
 # ---------------------------------------------------------------- served workload

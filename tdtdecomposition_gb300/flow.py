@@ -133,15 +133,20 @@ def all_affect_support_not_before(e_affect, graph, n_cut, mask, l, n_mark, suppo
     return n_mark, support
 
 
-def k_truss(graph, n_cut, num_v, cpu_flow=False, compact_threshold=1000000, fused=True):
+def k_truss(graph, n_cut, num_v, cpu_flow=False, compact_threshold=1000000, fused=True, fused_support=None,
+            fused_update=None):
     """singlegpu_truss.py:67-158 (cpu_flow=False, peel update = *_not) or
     test/truss_setup.py:61-154 (cpu_flow=True, peel update = sub_AllAffectedSupport*).
     fused=False runs the fusion experiment's unfused operators instead
     (support_computing_before, all_affect_support_not_before;
-    fusionexperiental.py:24-67) with the same results.
+    fusionexperiental.py:24-67) with the same results; fused_support /
+    fused_update choose each half on its own (the four columns of the
+    reference's ablation: TDT-origin, +Comp, +Update, +both).
     Mutates graph like the reference.  Returns (kmax, e_truss, ptr_truss)."""
     dev = graph.device
-    if fused:
+    fused_support = fused if fused_support is None else fused_support
+    fused_update = fused if fused_update is None else fused_update
+    if fused_support:
         support = support_computing(graph.rows, graph.columns, graph.row_ptr, n_cut)
     else:
         support = support_computing_before(graph.rows, graph.columns, graph.row_ptr, n_cut)
@@ -177,7 +182,7 @@ def k_truss(graph, n_cut, num_v, cpu_flow=False, compact_threshold=1000000, fuse
         n_mark = torch.zeros(graph.columns.shape[0], dtype=torch.bool, device=dev)
         if cpu_flow:
             all_affect_support(e_affect, graph, n_cut, e_mask, l, n_mark, support)
-        elif fused:
+        elif fused_update:
             all_affect_support_not(e_affect, graph, n_cut, e_mask, l, n_mark, support)
         else:
             all_affect_support_not_before(e_affect, graph, n_cut, e_mask, l, n_mark, support)
