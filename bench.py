@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--fusion", action="store_true",
                     help="add the fusion-experiment line (unfused vs fused support count)")
     ap.add_argument("--fusion-scale", type=int, default=18)
+    ap.add_argument("--undirected", action="store_true",
+                    help="add the undirected-driver line (oriented and symmetric peel updates)")
     return ap.parse_args()
 
 
@@ -387,6 +389,53 @@ def bench_fusion(dev, scale=18, reps=3):
     return out
 
 
+# ---------------------------------------------------------------- undirected drivers
+def bench_undirected(dev, scale=18):
+    """The reference's undirected-graph drivers (truss_undirect_cuda2.py with
+    the oriented peel updates, truss_undirect_cuda.py with the symmetric one)
+    restated over this library's operators, on R-MAT scale `scale`, edge
+    factor 16, seed 1, n_cut 1; one run each after a warm-up, checked against
+    the device-resident decomposition (same kmax, same per-edge truss)."""
+    import torch
+    from tdtdecomposition_gb300 import flow, generators as G, truss as T
+    from tdtdecomposition_gb300.preprocess import preprocess_edges
+    src, dst = G.rmat_edges_device(scale, 16 << scale, seed=1, device=dev)
+    g, _ = preprocess_edges(src, dst)
+    del src, dst
+    res = T.truss_decompose(g)
+    E = g.num_edges
+
+    def truss_of(e, p):
+        t = torch.full((E,), 2, dtype=torch.int32, device=dev)
+        lv = torch.repeat_interleave(torch.arange(p.numel() - 1, device=dev, dtype=torch.int32) + 3,
+                                     (p[1:] - p[:-1]).to(dev).long())
+        t[e.long()] = lv
+        return t
+
+    out = {"workload": "R-MAT scale %d, edge factor 16, seed 1" % scale, "E": E, "kmax": res.kmax}
+    runs = (("oriented (peeling_direct_oo/ii/oi)",
+             lambda: flow.undirected_truss_direct(g, *flow.preprocess_direct(g, 1), 1)),
+            ("symmetric (peeling_undirect)",
+             lambda: (lambda parts: flow.undirected_truss_undirect(g, parts[1], parts[2], parts[0], parts[3], 1, 1))(
+                 flow.preprocess_undirect(g, 1, 1))))
+    for name, fn in runs:
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        k, e, p = fn()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        if k != res.kmax or not torch.equal(truss_of(e, p), res.truss):
+            raise SystemExit("undirected driver %s differs from the decomposition" % name)
+        out[name] = {"s": dt, "edges_per_s": E / dt}
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    T.truss_decompose(g)
+    torch.cuda.synchronize()
+    out["device-resident s"] = time.perf_counter() - t
+    return out
+
+
 # ---------------------------------------------------------------- served workload
 def bench_served(dev, n_requests=48, rates=(8.0, 32.0, 128.0)):
     """Poisson request streams (the same 48 seeded requests replayed at each
@@ -640,6 +689,8 @@ def main_ours(args):
         line["skewed"] = bench_skewed(dev, args.skewed_log2n)
     if args.fusion:
         line["fusion"] = bench_fusion(dev, args.fusion_scale)
+    if args.undirected:
+        line["undirected"] = bench_undirected(dev, args.fusion_scale)
     if not args.no_cpu_baseline:
         sc = cpu_sample_scale(args, 1)
         Ec, Vc, times, threads = cpu_decompose_sample(sc, 1)
