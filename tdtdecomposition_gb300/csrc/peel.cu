@@ -202,6 +202,108 @@ __device__ __forceinline__ void warp_append2(const PeelArgs& A, int slot, int bu
     }
 }
 
+// Sub-round appends are staged per warp in shared memory and reserved in the
+// queue in batches: one queue atomic (and one frontier-count atomic) per
+// flush instead of two per warp step that marks an edge, which keeps the
+// reservation's round trip and the contention on the round's counters out of
+// most steps.  The queue order of items changes nothing: a sub-round is a set.
+#ifndef TDT_APPEND_BUF
+#define TDT_APPEND_BUF 64
+#endif
+constexpr int kAppBuf = TDT_APPEND_BUF;  // entries per warp; a flush leaves room for one 64-edge append
+static_assert(kAppBuf >= 64 && kAppBuf % 32 == 0, "append buffer");
+
+struct AppendBuf {
+    int4* it;                    // this warp's staged items (shared memory)
+    int* dx;                     // their candidate counts
+    int n;                       // staged items (warp-uniform)
+    unsigned long long nfront;   // edges marked since the last flush (warp-uniform)
+};
+
+__device__ __noinline__ void append_flush(const PeelArgs& A, int slot, int buf, AppendBuf& B,
+                                          unsigned long long* nfront) {
+    const unsigned lane = lane_id();
+    __syncwarp();
+    if (B.nfront) {
+        if (lane == 0) atomicAdd(nfront, B.nfront);
+        B.nfront = 0;
+    }
+    if (B.n > 0) {
+        constexpr int kPer = kAppBuf / kWarp;
+        const int i0 = (int)lane * kPer;
+        long long sum = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) sum += i0 + k < B.n ? B.dx[i0 + k] : 0;
+        const long long incl = warp_incl_scan(sum);
+        const long long tot = __shfl_sync(kFull, incl, 31);
+        const unsigned long long old = reserve_items(A, slot, B.n, tot);
+        long long idx = (long long)(old >> kCandBits) + i0;
+        long long cc = (long long)(old & kCandMask) + incl - sum;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            if (i0 + k < B.n && idx < A.E) {
+                A.qi[buf][idx] = B.it[i0 + k];
+                A.qb[buf][idx] = cc;
+                cc += B.dx[i0 + k];
+            }
+            idx++;
+        }
+        B.n = 0;
+    }
+    __syncwarp();
+}
+
+// Stage up to two edges per lane (f, g of one triangle) for the round in `slot`.
+template <bool Listed>
+__device__ __forceinline__ void warp_append2_staged(const PeelArgs& A, int slot, int buf, bool wf, int32_t f,
+                                                    bool wg, int32_t g, int32_t cur_sup, AppendBuf& B,
+                                                    unsigned long long* nfront) {
+    const unsigned mf = __ballot_sync(kFull, wf), mg = __ballot_sync(kFull, wg);
+    if ((mf | mg) == 0) return;
+    B.nfront += (unsigned long long)(__popc(mf) + __popc(mg));
+    int4 itf, itg;
+    long long dxf, dxg;
+    const bool qf = make_item<Listed>(A, wf, cur_sup, f, itf, dxf);
+    const bool qg = make_item<Listed>(A, wg, cur_sup, g, itg, dxg);
+    const int nq = (qf ? 1 : 0) + (qg ? 1 : 0);
+    const int nincl = warp_incl_scan(nq);
+    const int ntot = __shfl_sync(kFull, nincl, 31);
+    if (ntot == 0) return;
+    if (B.n + ntot > kAppBuf) append_flush(A, slot, buf, B, nfront);
+    int p = B.n + nincl - nq;
+    if (qf) {
+        B.it[p] = itf;
+        B.dx[p] = (int)dxf;
+        p++;
+    }
+    if (qg) {
+        B.it[p] = itg;
+        B.dx[p] = (int)dxg;
+    }
+    B.n += ntot;
+}
+
+// Stage the edges flagged by `want` (one per lane); cur_sup as in warp_append.
+__device__ __forceinline__ void warp_append_staged(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
+                                                   int32_t cur_sup, AppendBuf& B, unsigned long long* nfront) {
+    const unsigned mf = __ballot_sync(kFull, want);
+    if (mf == 0) return;
+    B.nfront += (unsigned long long)__popc(mf);
+    int4 it;
+    long long dx;
+    const bool q = A.lists ? make_item<true>(A, want, cur_sup, e, it, dx) : make_item<false>(A, want, cur_sup, e, it, dx);
+    const unsigned m = __ballot_sync(kFull, q);
+    if (m == 0) return;
+    const int ntot = __popc(m);
+    if (B.n + ntot > kAppBuf) append_flush(A, slot, buf, B, nfront);
+    if (q) {
+        const int p = B.n + __popc(m & lanemask_lt());
+        B.it[p] = it;
+        B.dx[p] = (int)dx;
+    }
+    B.n += ntot;
+}
+
 // Level changes (decomposition mode).  Level change t starts level L_t =
 // min support over the alive edges and queues F = alive edges with support
 // L_t.  The alive edges live in a compacted list (list t&1 is the input of
@@ -248,7 +350,8 @@ __device__ __forceinline__ void pass_start(const PeelArgs& A, int np) {
     }
 }
 
-__device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int t, int& np, int32_t* l_out) {
+__device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int t, int& np, int32_t* l_out,
+                                              int4* app_it, int* app_dx) {
     const unsigned lane = lane_id();
     const long long gw = (long long)blockIdx.x * kPeelWarps + threadIdx.x / kWarp;
     const long long nw = (long long)gridDim.x * kPeelWarps;
@@ -266,6 +369,7 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
     const int32_t gw_end = g > INT32_MAX - kSideWindow ? INT32_MAX : g + kSideWindow;
     const int slot = r_next % 3, buf = r_next & 1;
     int2* side = reinterpret_cast<int2*>(A.qi[buf ^ 1]);  // the finished round's queue is free
+    AppendBuf B{app_it + (threadIdx.x / kWarp) * kAppBuf, app_dx + (threadIdx.x / kWarp) * kAppBuf, 0, 0ull};
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         A.ctl->cnt[(t + 1) % 3] = 0;
         A.ctl->dmin[t & 1] = INT32_MAX;
@@ -342,10 +446,11 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
                 os += __popc(wm[u]);
                 const bool want = keep[u] && sv[u] == g;
                 if (want) A.es[e[u]].y = r_next;
-                warp_append(A, slot, buf, want, e[u], sv[u], &A.ctl->pfe[np % 3]);
+                warp_append_staged(A, slot, buf, want, e[u], sv[u], B, &A.ctl->pfe[np % 3]);
             }
             __syncthreads();  // s_tk / s_base are reused by the next tile
         }
+        append_flush(A, slot, buf, B, &A.ctl->pfe[np % 3]);
         pass_min(A, np, mloc);
     }
     np++;
@@ -375,7 +480,7 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
             const bool want = i < ns && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
             if (want) A.es[e].y = r_next;
-            warp_append(A, slot, buf, want, e, sv, &A.ctl->pfe[np % 3]);
+            warp_append_staged(A, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
         }
     } else {
         // pass 2b: one more pass over the compacted list
@@ -390,9 +495,10 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
             const bool want = i < n2 && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
             if (want) A.es[e].y = r_next;
-            warp_append(A, slot, buf, want, e, sv, &A.ctl->pfe[np % 3]);
+            warp_append_staged(A, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
         }
     }
+    append_flush(A, slot, buf, B, &A.ctl->pfe[np % 3]);
     pass_min(A, np, mloc);
     np++;
     return grid_barrier(&A.ctl->g, gridDim.x);
@@ -544,12 +650,14 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
 // so its registers are allocated apart from the persistent loop around it.
 template <bool Listed>
 __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp, long long nwarps,
-                                           int* dmin) {
+                                           int* dmin, int4* app_it, int* app_dx) {
     const unsigned lane = lane_id();
     const unsigned le = lanemask_lt() | (1u << lane);
     int32_t dm = INT32_MAX;
     const int slot = r % 3, buf = r & 1;
     const int nslot = (r + 1) % 3, nbuf = buf ^ 1;
+    const int wib = threadIdx.x / kWarp;
+    AppendBuf B{app_it + wib * kAppBuf, app_dx + wib * kAppBuf, 0, 0ull};
     const unsigned long long packed = ld_cg_u64(&A.ctl->q[slot]);
     const long long N = (long long)(packed >> kCandBits);
     const long long T = (long long)(packed & kCandMask);
@@ -630,8 +738,8 @@ __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, 
         if (wga) A.es[ga].y = r + 1;
         if (wfb) A.es[fb].y = r + 1;
         if (wgb) A.es[gb].y = r + 1;
-        warp_append2<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, &A.ctl->fe[nslot]);
-        warp_append2<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, &A.ctl->fe[nslot]);
+        warp_append2_staged<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, B, &A.ctl->fe[nslot]);
+        warp_append2_staged<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, B, &A.ctl->fe[nslot]);
         if (has_b) {
             i0 = wb.i0n;
             base0 = wb.base0n;
@@ -640,6 +748,7 @@ __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, 
             base0 = wa.base0n;
         }
     }
+    append_flush(A, nslot, nbuf, B, &A.ctl->fe[nslot]);
     fold_min(dmin, dm);
 }
 
@@ -647,6 +756,8 @@ __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, 
 #define TDT_PEEL_MINB 2
 #endif
 __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArgs A) {
+    __shared__ int4 s_app_it[kPeelWarps * kAppBuf];  // per-warp append staging of the sub-rounds
+    __shared__ int s_app_dx[kPeelWarps * kAppBuf];
     if (!*(volatile int*)&A.ctl->listed) A.lists = nullptr;
     const bool listed = A.lists != nullptr;
     const int wib = threadIdx.x / kWarp;
@@ -661,7 +772,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
     int ntrans = 0, np = 0;
     bool ok;
     if (A.mode == 0) {
-        ok = level_transition(A, 0, ntrans++, np, &l);
+        ok = level_transition(A, 0, ntrans++, np, &l, s_app_it, s_app_dx);
     } else {
         l = A.fixed_level;
         ok = fixed_collect(A, l, 0, np);
@@ -679,8 +790,8 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
             if (globaltimer_ns() - t_start > A.deadline_ns) set_status(A.ctl, TDT_ERR_TIMEOUT);
         }
         // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
-        if (listed) process_round<true>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1]);
-        else process_round<false>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1]);
+        if (listed) process_round<true>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_it, s_app_dx);
+        else process_round<false>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_it, s_app_dx);
         __syncthreads();
         const uint64_t t_p = globaltimer_ns();
         if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
@@ -704,7 +815,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
                 continue;
             }
             int32_t nl;
-            const bool more = level_transition(A, r + 1, ntrans++, np, &nl);
+            const bool more = level_transition(A, r + 1, ntrans++, np, &nl, s_app_it, s_app_dx);
             if (master) A.ctl->t_trans += globaltimer_ns() - t_b;
             if (!more) break;
             l = nl;
