@@ -214,13 +214,16 @@ __device__ __forceinline__ void resolve(const OutRows<Off>& G, const SupArgs& A,
     }
 }
 
+// Positions in cols are int32: edge ids are int32 throughout (the whole-path
+// calls reject E >= 2^31 and the drop-in operators take int32 row_ptr).
+//
 // Walk wedges [w0, w1) of a group: S[0..n) are the strictly increasing starts
 // of the group's non-empty out-lists in the flat wedge space, BV their
 // positions in cols, VI the index of their v in N+(u).  w0 is a multiple of
 // 32 and o0 the group entry that holds wedge w0.
 template <int M, bool kIdOrdered, class Off>
 __device__ __forceinline__ void walk_group(const OutRows<Off>& G, const SupArgs& A, const RowState& R,
-                                           const int32_t* S, const int32_t* VI, const Off* BV, int n, int w0, int w1,
+                                           const int32_t* S, const int32_t* VI, const int32_t* BV, int n, int w0, int w1,
                                            int o0, WarpQueue& Q) {
     const unsigned lane = lane_id();
     const unsigned lt = lanemask_lt();
@@ -239,7 +242,7 @@ __device__ __forceinline__ void walk_group(const OutRows<Off>& G, const SupArgs&
         int vi = 0;
         if (t < w1) {
             const int o = ob + __popc(mk & (lt | (1u << lane)));
-            const Off pos = BV[o] + (Off)(t - S[o]);
+            const int32_t pos = BV[o] + (t - S[o]);
             const int32_t w = __ldg(G.cols + pos);
             if (w <= R.umax) {
                 const uint32_t h = bm_hash(w, R.bm_log2);
@@ -382,7 +385,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
         uint32_t* h_cnt = reinterpret_cast<uint32_t*>(smem + 4 * kHeavyCap);
         int32_t* g_S = reinterpret_cast<int32_t*>(smem + kHvS);
         int32_t* g_VI = reinterpret_cast<int32_t*>(smem + kHvVI);
-        Off* g_BV = reinterpret_cast<Off*>(smem + kHvBV);
+        int32_t* g_BV = reinterpret_cast<int32_t*>(smem + kHvBV);
         WarpQueue Q;
         Q.pos = reinterpret_cast<int32_t*>(smem + kHvQueues + wib * 8 * kQueue);
         Q.vi = Q.pos + kQueue;
@@ -416,11 +419,11 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                     // group: v's g0 .. g0+511, one per thread
                     const int i = g0 + threadIdx.x;
                     int32_t len = 0;
-                    Off bv = 0;
+                    int32_t bv = 0;
                     if (i < vend) {
                         const int32_t v = R.su[i];
                         if (v >= 0 && v < nv) {
-                            bv = G.begin(v);
+                            bv = (int32_t)G.begin(v);
                             len = (int32_t)(G.end(v) - bv);
                         }
                     }
@@ -488,7 +491,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
     uint32_t* l_cnt = reinterpret_cast<uint32_t*>(sl + kSlCnt);
     int32_t* l_S = reinterpret_cast<int32_t*>(sl + kSlS);
     int32_t* l_VI = reinterpret_cast<int32_t*>(sl + kSlVI);
-    Off* l_BV = reinterpret_cast<Off*>(sl + kSlBV);
+    int32_t* l_BV = reinterpret_cast<int32_t*>(sl + kSlBV);
     uint32_t* l_bm = reinterpret_cast<uint32_t*>(sl + kSlBm);
     WarpQueue Q;
     Q.pos = reinterpret_cast<int32_t*>(sl + kSlQ);
@@ -517,11 +520,11 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
             for (int vb = 0; vb < vend; vb += kWarp) {
                 const int i = vb + (int)lane;
                 int32_t len = 0;
-                Off bv = 0;
+                int32_t bv = 0;
                 if (i < vend) {
                     const int32_t v = l_su[i];
                     if (v >= 0 && v < nv) {
-                        bv = G.begin(v);
+                        bv = (int32_t)G.begin(v);
                         len = (int32_t)(G.end(v) - bv);
                     }
                 }
