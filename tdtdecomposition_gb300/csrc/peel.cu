@@ -137,71 +137,6 @@ __device__ __forceinline__ unsigned long long reserve_items(const PeelArgs& A, i
     return __shfl_sync(kFull, old, 0);
 }
 
-// Queue the edges flagged by `want` (one per lane) for the round in `slot`
-// and add their number to *nfront.  cur_sup is the edge's support at marking
-// time (0 => no alive triangle).
-__device__ __forceinline__ void warp_append(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
-                                            int32_t cur_sup, unsigned long long* nfront) {
-    const unsigned lane = lane_id();
-    const unsigned mf = __ballot_sync(kFull, want);
-    if (mf == 0) return;
-    if (lane == (unsigned)(__ffs(mf) - 1)) atomicAdd(nfront, (unsigned long long)__popc(mf));
-    int4 it;
-    long long dx;
-    const bool q = A.lists ? make_item<true>(A, want, cur_sup, e, it, dx) : make_item<false>(A, want, cur_sup, e, it, dx);
-    const unsigned m = __ballot_sync(kFull, q);
-    if (m == 0) return;
-    const long long c = q ? dx : 0;
-    const long long incl = warp_incl_scan(c);
-    const long long tot = __shfl_sync(kFull, incl, 31);
-    const unsigned long long old = reserve_items(A, slot, __popc(m), tot);
-    if (q) {
-        const long long it0 = (long long)(old >> kCandBits), c0 = (long long)(old & kCandMask);
-        const long long idx = it0 + __popc(m & lanemask_lt());
-        if (idx < A.E) {
-            A.qi[buf][idx] = it;
-            A.qb[buf][idx] = c0 + incl - c;
-        }
-    }
-}
-
-// The same for up to two edges per lane (f, g of one triangle), with one
-// reservation for the warp.
-template <bool Listed>
-__device__ __forceinline__ void warp_append2(const PeelArgs& A, int slot, int buf, bool wf, int32_t f, bool wg,
-                                             int32_t g, int32_t cur_sup, unsigned long long* nfront) {
-    const unsigned lane = lane_id();
-    const unsigned mf = __ballot_sync(kFull, wf), mg = __ballot_sync(kFull, wg);
-    if ((mf | mg) == 0) return;
-    if (lane == 0) atomicAdd(nfront, (unsigned long long)(__popc(mf) + __popc(mg)));
-    int4 itf, itg;
-    long long dxf, dxg;
-    const bool qf = make_item<Listed>(A, wf, cur_sup, f, itf, dxf);
-    const bool qg = make_item<Listed>(A, wg, cur_sup, g, itg, dxg);
-    const int nq = (qf ? 1 : 0) + (qg ? 1 : 0);
-    if (__ballot_sync(kFull, nq > 0) == 0) return;
-    const long long c = (qf ? dxf : 0) + (qg ? dxg : 0);
-    const int nincl = warp_incl_scan(nq);
-    const long long cincl = warp_incl_scan(c);
-    const int ntot = __shfl_sync(kFull, nincl, 31);
-    const long long ctot = __shfl_sync(kFull, cincl, 31);
-    const unsigned long long old = reserve_items(A, slot, ntot, ctot);
-    long long idx = (long long)(old >> kCandBits) + nincl - nq;
-    long long cc = (long long)(old & kCandMask) + cincl - c;
-    if (qf) {
-        if (idx < A.E) {
-            A.qi[buf][idx] = itf;
-            A.qb[buf][idx] = cc;
-        }
-        idx++;
-        cc += dxf;
-    }
-    if (qg && idx < A.E) {
-        A.qi[buf][idx] = itg;
-        A.qb[buf][idx] = cc;
-    }
-}
-
 // Sub-round appends are staged per warp in shared memory and reserved in the
 // queue in batches: one queue atomic (and one frontier-count atomic) per
 // flush instead of two per warp step that marks an edge, which keeps the
@@ -283,7 +218,8 @@ __device__ __forceinline__ void warp_append2_staged(const PeelArgs& A, int slot,
     B.n += ntot;
 }
 
-// Stage the edges flagged by `want` (one per lane); cur_sup as in warp_append.
+// Stage the edges flagged by `want` (one per lane) for the round in `slot`.
+// cur_sup is the edge's support at marking time (0 => no alive triangle).
 __device__ __forceinline__ void warp_append_staged(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
                                                    int32_t cur_sup, AppendBuf& B, unsigned long long* nfront) {
     const unsigned mf = __ballot_sync(kFull, want);
