@@ -155,7 +155,7 @@ struct AppendBuf {
     unsigned long long nfront;   // edges marked since the last flush (warp-uniform)
 };
 
-__device__ __noinline__ void append_flush(const PeelArgs& A, int slot, int buf, AppendBuf& B,
+__device__ __forceinline__ void append_flush(const PeelArgs& A, int slot, int buf, AppendBuf& B,
                                           unsigned long long* nfront) {
     const unsigned lane = lane_id();
     __syncwarp();
@@ -220,14 +220,15 @@ __device__ __forceinline__ void warp_append2_staged(const PeelArgs& A, int slot,
 
 // Stage the edges flagged by `want` (one per lane) for the round in `slot`.
 // cur_sup is the edge's support at marking time (0 => no alive triangle).
-__device__ __forceinline__ void warp_append_staged(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
-                                                   int32_t cur_sup, AppendBuf& B, unsigned long long* nfront) {
+__device__ __forceinline__ void warp_append_staged(const PeelArgs& A, bool listed, int slot, int buf, bool want,
+                                                   int32_t e, int32_t cur_sup, AppendBuf& B,
+                                                   unsigned long long* nfront) {
     const unsigned mf = __ballot_sync(kFull, want);
     if (mf == 0) return;
     B.nfront += (unsigned long long)__popc(mf);
     int4 it;
     long long dx;
-    const bool q = A.lists ? make_item<true>(A, want, cur_sup, e, it, dx) : make_item<false>(A, want, cur_sup, e, it, dx);
+    const bool q = listed ? make_item<true>(A, want, cur_sup, e, it, dx) : make_item<false>(A, want, cur_sup, e, it, dx);
     const unsigned m = __ballot_sync(kFull, q);
     if (m == 0) return;
     const int ntot = __popc(m);
@@ -286,8 +287,8 @@ __device__ __forceinline__ void pass_start(const PeelArgs& A, int np) {
     }
 }
 
-__device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int t, int& np, int32_t* l_out,
-                                              int4* app_it, int* app_dx) {
+__device__ __noinline__ bool level_transition(const PeelArgs& A, bool listed, int r_next, int t, int& np,
+                                              int32_t* l_out, int4* app_it, int* app_dx) {
     const unsigned lane = lane_id();
     const long long gw = (long long)blockIdx.x * kPeelWarps + threadIdx.x / kWarp;
     const long long nw = (long long)gridDim.x * kPeelWarps;
@@ -382,7 +383,7 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
                 os += __popc(wm[u]);
                 const bool want = keep[u] && sv[u] == g;
                 if (want) A.es[e[u]].y = r_next;
-                warp_append_staged(A, slot, buf, want, e[u], sv[u], B, &A.ctl->pfe[np % 3]);
+                warp_append_staged(A, listed, slot, buf, want, e[u], sv[u], B, &A.ctl->pfe[np % 3]);
             }
             __syncthreads();  // s_tk / s_base are reused by the next tile
         }
@@ -416,7 +417,7 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
             const bool want = i < ns && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
             if (want) A.es[e].y = r_next;
-            warp_append_staged(A, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
+            warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
         }
     } else {
         // pass 2b: one more pass over the compacted list
@@ -431,7 +432,7 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
             const bool want = i < n2 && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
             if (want) A.es[e].y = r_next;
-            warp_append_staged(A, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
+            warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
         }
     }
     append_flush(A, slot, buf, B, &A.ctl->pfe[np % 3]);
@@ -452,13 +453,14 @@ __device__ __noinline__ bool level_transition(const PeelArgs& A, int r_next, int
 constexpr unsigned long long kFixedItemCap = 1ull << 27;
 constexpr unsigned long long kFixedCandCap = 1ull << 35;
 
-__device__ __forceinline__ void warp_append_capped(const PeelArgs& A, int slot, int buf, bool want, int32_t e,
+__device__ __forceinline__ void warp_append_capped(const PeelArgs& A, bool listed, int slot, int buf, bool want,
+                                                   int32_t e,
                                                    int32_t s, int r_next, unsigned long long* nfront) {
     const unsigned lane = lane_id();
     if (__ballot_sync(kFull, want) == 0) return;
     int4 it;
     long long dx;
-    const bool q = A.lists ? make_item<true>(A, want, s, e, it, dx) : make_item<false>(A, want, s, e, it, dx);
+    const bool q = listed ? make_item<true>(A, want, s, e, it, dx) : make_item<false>(A, want, s, e, it, dx);
     const unsigned m = __ballot_sync(kFull, q);
     const long long c = q ? dx : 0;
     const long long incl = warp_incl_scan(c);
@@ -496,7 +498,7 @@ __device__ __forceinline__ void warp_append_capped(const PeelArgs& A, int slot, 
 }
 
 // One collection pass for sub-round r_next; true when it took an edge.
-__device__ bool fixed_collect(const PeelArgs& A, int32_t l, int r_next, int& np) {
+__device__ bool fixed_collect(const PeelArgs& A, bool listed, int32_t l, int r_next, int& np) {
     const unsigned lane = lane_id();
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
     const int slot = r_next % 3, buf = r_next & 1;
@@ -511,7 +513,7 @@ __device__ bool fixed_collect(const PeelArgs& A, int32_t l, int r_next, int& np)
             s = st.x;
             want = st.y == -1 && s <= l;
         }
-        warp_append_capped(A, slot, buf, want, (int32_t)e, s, r_next, &A.ctl->pfe[np % 3]);
+        warp_append_capped(A, listed, slot, buf, want, (int32_t)e, s, r_next, &A.ctl->pfe[np % 3]);
     }
     np++;
     if (!grid_barrier(&A.ctl->g, gridDim.x)) return false;
@@ -691,11 +693,12 @@ __device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, 
 #ifndef TDT_PEEL_MINB
 #define TDT_PEEL_MINB 2
 #endif
-__global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArgs A) {
+// A is a __grid_constant__ parameter: the helpers take it by reference and
+// read its fields from the parameter bank instead of a local copy.
+__global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const __grid_constant__ PeelArgs A) {
     __shared__ int4 s_app_it[kPeelWarps * kAppBuf];  // per-warp append staging of the sub-rounds
     __shared__ int s_app_dx[kPeelWarps * kAppBuf];
-    if (!*(volatile int*)&A.ctl->listed) A.lists = nullptr;
-    const bool listed = A.lists != nullptr;
+    const bool listed = A.lists != nullptr && *(volatile int*)&A.ctl->listed != 0;
     const int wib = threadIdx.x / kWarp;
     const int64_t gwarp = (int64_t)blockIdx.x * kPeelWarps + wib;
     const int64_t nwarps = (int64_t)gridDim.x * kPeelWarps;
@@ -708,10 +711,10 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
     int ntrans = 0, np = 0;
     bool ok;
     if (A.mode == 0) {
-        ok = level_transition(A, 0, ntrans++, np, &l, s_app_it, s_app_dx);
+        ok = level_transition(A, listed, 0, ntrans++, np, &l, s_app_it, s_app_dx);
     } else {
         l = A.fixed_level;
-        ok = fixed_collect(A, l, 0, np);
+        ok = fixed_collect(A, listed, l, 0, np);
     }
     if (!ok) {
         if (master) A.ctl->rounds = 0;
@@ -745,13 +748,13 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(PeelArg
         if (ld_cg_u64(&A.ctl->fe[(r + 1) % 3]) == 0) {
             if (A.mode != 0) {
                 // k-truss search: the next batch of low-support edges, if any
-                if (!fixed_collect(A, l, r + 1, np)) break;
+                if (!fixed_collect(A, listed, l, r + 1, np)) break;
                 t_mark = globaltimer_ns();
                 r++;
                 continue;
             }
             int32_t nl;
-            const bool more = level_transition(A, r + 1, ntrans++, np, &nl, s_app_it, s_app_dx);
+            const bool more = level_transition(A, listed, r + 1, ntrans++, np, &nl, s_app_it, s_app_dx);
             if (master) A.ctl->t_trans += globaltimer_ns() - t_b;
             if (!more) break;
             l = nl;
