@@ -287,7 +287,7 @@ __device__ __forceinline__ void pass_start(const PeelArgs& A, int np) {
     }
 }
 
-__device__ __noinline__ bool level_transition(const PeelArgs& A, bool listed, int r_next, int t, int& np,
+__device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed, int r_next, int t, int& np,
                                               int32_t* l_out, int4* app_it, int* app_dx) {
     const unsigned lane = lane_id();
     const long long gw = (long long)blockIdx.x * kPeelWarps + threadIdx.x / kWarp;
@@ -584,10 +584,12 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
 // One sub-round: warps gwarp = 0..nwarps-1 share the candidate slots of round r.
 // The smallest decrement result above l is folded into *dmin (the lower bound
 // of the next level).  Each step covers two 32-slot windows whose loads and
-// decrements are in flight together.  Compiled once per mode and not inlined,
-// so its registers are allocated apart from the persistent loop around it.
+// decrements are in flight together.  Inlined into the persistent loop (with
+// the level changes): the kernel arguments are a __grid_constant__ parameter,
+// so no call passes a local copy of them, and no call frame is saved around
+// every sub-round.
 template <bool Listed>
-__device__ __noinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp, long long nwarps,
+__device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp, long long nwarps,
                                            int* dmin, int4* app_it, int* app_dx) {
     const unsigned lane = lane_id();
     const unsigned le = lanemask_lt() | (1u << lane);
