@@ -236,7 +236,7 @@ __device__ __forceinline__ void on_shared(const PeelOpArgs& A, int32_t e, int32_
 }
 
 template <int V>
-__global__ void __launch_bounds__(kRBlock) peel_op_kernel(PeelOpArgs A) {
+__global__ void __launch_bounds__(kRBlock) peel_op_kernel(const __grid_constant__ PeelOpArgs A) {
     constexpr int KA = V == kVarII ? kIn : (V == kVarUnd ? kUnd : kOut);
     constexpr int KB = V == kVarOO ? kOut : (V == kVarUnd ? kUnd : kIn);
     __shared__ int32_t s_key[kRWarps][kRSlots];
