@@ -149,14 +149,16 @@ constexpr int kAppBuf = TDT_APPEND_BUF;  // entries per warp; a flush leaves roo
 static_assert(kAppBuf >= 64 && kAppBuf % 32 == 0, "append buffer");
 
 struct AppendBuf {
-    int4* it;                    // this warp's staged items (shared memory)
-    int* dx;                     // their candidate counts
-    int n;                       // staged items (warp-uniform)
+    int32_t* e;                  // this warp's staged edges (shared memory)
+    int n;                       // staged edges (warp-uniform)
     unsigned long long nfront;   // edges marked since the last flush (warp-uniform)
 };
 
+// Queue the staged edges: their items are built here (kAppBuf / 32 per lane),
+// reserved with one atomic and written.
+template <bool Listed>
 __device__ __forceinline__ void append_flush(const PeelArgs& A, int slot, int buf, AppendBuf& B,
-                                          unsigned long long* nfront) {
+                                             unsigned long long* nfront) {
     const unsigned lane = lane_id();
     __syncwarp();
     if (B.nfront) {
@@ -165,30 +167,54 @@ __device__ __forceinline__ void append_flush(const PeelArgs& A, int slot, int bu
     }
     if (B.n > 0) {
         constexpr int kPer = kAppBuf / kWarp;
-        const int i0 = (int)lane * kPer;
+        int4 it[kPer];
+        long long dx[kPer];
+        bool q[kPer];
+        int nq = 0;
         long long sum = 0;
 #pragma unroll
-        for (int k = 0; k < kPer; k++) sum += i0 + k < B.n ? B.dx[i0 + k] : 0;
-        const long long incl = warp_incl_scan(sum);
-        const long long tot = __shfl_sync(kFull, incl, 31);
-        const unsigned long long old = reserve_items(A, slot, B.n, tot);
-        long long idx = (long long)(old >> kCandBits) + i0;
-        long long cc = (long long)(old & kCandMask) + incl - sum;
-#pragma unroll
         for (int k = 0; k < kPer; k++) {
-            if (i0 + k < B.n && idx < A.E) {
-                A.qi[buf][idx] = B.it[i0 + k];
-                A.qb[buf][idx] = cc;
-                cc += B.dx[i0 + k];
+            const int i = (int)lane * kPer + k;
+            q[k] = i < B.n && make_item<Listed>(A, true, 1, B.e[i], it[k], dx[k]);
+            if (q[k]) {
+                nq++;
+                sum += dx[k];
             }
-            idx++;
+        }
+        const int nincl = warp_incl_scan(nq);
+        const int ntot = __shfl_sync(kFull, nincl, 31);
+        const long long cincl = warp_incl_scan(sum);
+        const long long ctot = __shfl_sync(kFull, cincl, 31);
+        if (ntot > 0) {
+            const unsigned long long old = reserve_items(A, slot, ntot, ctot);
+            long long idx = (long long)(old >> kCandBits) + nincl - nq;
+            long long cc = (long long)(old & kCandMask) + cincl - sum;
+#pragma unroll
+            for (int k = 0; k < kPer; k++) {
+                if (q[k]) {
+                    if (idx < A.E) {
+                        A.qi[buf][idx] = it[k];
+                        A.qb[buf][idx] = cc;
+                    }
+                    idx++;
+                    cc += dx[k];
+                }
+            }
         }
         B.n = 0;
     }
     __syncwarp();
 }
 
-// Stage up to two edges per lane (f, g of one triangle) for the round in `slot`.
+// The same as a call (the level-change passes: several call sites, rare flushes).
+template <bool Listed>
+__device__ __noinline__ void append_flush_call(const PeelArgs& A, int slot, int buf, AppendBuf& B,
+                                               unsigned long long* nfront) {
+    append_flush<Listed>(A, slot, buf, B, nfront);
+}
+
+// Stage up to two edges per lane (f, g of one triangle) for the round in
+// `slot`; cur_sup (the level, warp-uniform) <= 0 queues no item.
 template <bool Listed>
 __device__ __forceinline__ void warp_append2_staged(const PeelArgs& A, int slot, int buf, bool wf, int32_t f,
                                                     bool wg, int32_t g, int32_t cur_sup, AppendBuf& B,
@@ -196,26 +222,54 @@ __device__ __forceinline__ void warp_append2_staged(const PeelArgs& A, int slot,
     const unsigned mf = __ballot_sync(kFull, wf), mg = __ballot_sync(kFull, wg);
     if ((mf | mg) == 0) return;
     B.nfront += (unsigned long long)(__popc(mf) + __popc(mg));
+    if (cur_sup <= 0) return;
+    const int nq = (wf ? 1 : 0) + (wg ? 1 : 0);
+    const int nincl = warp_incl_scan(nq);
+    const int ntot = __shfl_sync(kFull, nincl, 31);
+    if (B.n + ntot > kAppBuf) append_flush<Listed>(A, slot, buf, B, nfront);
+    int p = B.n + nincl - nq;
+    if (wf) B.e[p++] = f;
+    if (wg) B.e[p] = g;
+    B.n += ntot;
+}
+
+// Queue up to two edges per lane directly, with one reservation per warp step
+// (the search-mode sub-rounds: their steps are long and append rarely, and the
+// staging state would stay live across the binary searches).
+template <bool Listed>
+__device__ __forceinline__ void warp_append2_direct(const PeelArgs& A, int slot, int buf, bool wf, int32_t f,
+                                                    bool wg, int32_t g, int32_t cur_sup,
+                                                    unsigned long long* nfront) {
+    const unsigned lane = lane_id();
+    const unsigned mf = __ballot_sync(kFull, wf), mg = __ballot_sync(kFull, wg);
+    if ((mf | mg) == 0) return;
+    if (lane == 0) atomicAdd(nfront, (unsigned long long)(__popc(mf) + __popc(mg)));
     int4 itf, itg;
     long long dxf, dxg;
     const bool qf = make_item<Listed>(A, wf, cur_sup, f, itf, dxf);
     const bool qg = make_item<Listed>(A, wg, cur_sup, g, itg, dxg);
     const int nq = (qf ? 1 : 0) + (qg ? 1 : 0);
+    if (__ballot_sync(kFull, nq > 0) == 0) return;
+    const long long c = (qf ? dxf : 0) + (qg ? dxg : 0);
     const int nincl = warp_incl_scan(nq);
+    const long long cincl = warp_incl_scan(c);
     const int ntot = __shfl_sync(kFull, nincl, 31);
-    if (ntot == 0) return;
-    if (B.n + ntot > kAppBuf) append_flush(A, slot, buf, B, nfront);
-    int p = B.n + nincl - nq;
+    const long long ctot = __shfl_sync(kFull, cincl, 31);
+    const unsigned long long old = reserve_items(A, slot, ntot, ctot);
+    long long idx = (long long)(old >> kCandBits) + nincl - nq;
+    long long cc = (long long)(old & kCandMask) + cincl - c;
     if (qf) {
-        B.it[p] = itf;
-        B.dx[p] = (int)dxf;
-        p++;
+        if (idx < A.E) {
+            A.qi[buf][idx] = itf;
+            A.qb[buf][idx] = cc;
+        }
+        idx++;
+        cc += dxf;
     }
-    if (qg) {
-        B.it[p] = itg;
-        B.dx[p] = (int)dxg;
+    if (qg && idx < A.E) {
+        A.qi[buf][idx] = itg;
+        A.qb[buf][idx] = cc;
     }
-    B.n += ntot;
 }
 
 // Stage the edges flagged by `want` (one per lane) for the round in `slot`.
@@ -226,18 +280,15 @@ __device__ __forceinline__ void warp_append_staged(const PeelArgs& A, bool liste
     const unsigned mf = __ballot_sync(kFull, want);
     if (mf == 0) return;
     B.nfront += (unsigned long long)__popc(mf);
-    int4 it;
-    long long dx;
-    const bool q = listed ? make_item<true>(A, want, cur_sup, e, it, dx) : make_item<false>(A, want, cur_sup, e, it, dx);
-    const unsigned m = __ballot_sync(kFull, q);
+    const bool st = want && cur_sup > 0;
+    const unsigned m = __ballot_sync(kFull, st);
     if (m == 0) return;
     const int ntot = __popc(m);
-    if (B.n + ntot > kAppBuf) append_flush(A, slot, buf, B, nfront);
-    if (q) {
-        const int p = B.n + __popc(m & lanemask_lt());
-        B.it[p] = it;
-        B.dx[p] = (int)dx;
+    if (B.n + ntot > kAppBuf) {
+        if (listed) append_flush_call<true>(A, slot, buf, B, nfront);
+        else append_flush_call<false>(A, slot, buf, B, nfront);
     }
+    if (st) B.e[B.n + __popc(m & lanemask_lt())] = e;
     B.n += ntot;
 }
 
@@ -288,7 +339,7 @@ __device__ __forceinline__ void pass_start(const PeelArgs& A, int np) {
 }
 
 __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed, int r_next, int t, int& np,
-                                              int32_t* l_out, int4* app_it, int* app_dx) {
+                                              int32_t* l_out, int32_t* app_e) {
     const unsigned lane = lane_id();
     const long long gw = (long long)blockIdx.x * kPeelWarps + threadIdx.x / kWarp;
     const long long nw = (long long)gridDim.x * kPeelWarps;
@@ -306,7 +357,7 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
     const int32_t gw_end = g > INT32_MAX - kSideWindow ? INT32_MAX : g + kSideWindow;
     const int slot = r_next % 3, buf = r_next & 1;
     int2* side = reinterpret_cast<int2*>(A.qi[buf ^ 1]);  // the finished round's queue is free
-    AppendBuf B{app_it + (threadIdx.x / kWarp) * kAppBuf, app_dx + (threadIdx.x / kWarp) * kAppBuf, 0, 0ull};
+    AppendBuf B{app_e + (threadIdx.x / kWarp) * kAppBuf, 0, 0ull};
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         A.ctl->cnt[(t + 1) % 3] = 0;
         A.ctl->dmin[t & 1] = INT32_MAX;
@@ -387,7 +438,8 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
             }
             __syncthreads();  // s_tk / s_base are reused by the next tile
         }
-        append_flush(A, slot, buf, B, &A.ctl->pfe[np % 3]);
+        if (listed) append_flush_call<true>(A, slot, buf, B, &A.ctl->pfe[np % 3]);
+        else append_flush_call<false>(A, slot, buf, B, &A.ctl->pfe[np % 3]);
         pass_min(A, np, mloc);
     }
     np++;
@@ -435,7 +487,8 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
             warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
         }
     }
-    append_flush(A, slot, buf, B, &A.ctl->pfe[np % 3]);
+    if (listed) append_flush_call<true>(A, slot, buf, B, &A.ctl->pfe[np % 3]);
+    else append_flush_call<false>(A, slot, buf, B, &A.ctl->pfe[np % 3]);
     pass_min(A, np, mloc);
     np++;
     return grid_barrier(&A.ctl->g, gridDim.x);
@@ -590,14 +643,14 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
 // every sub-round.
 template <bool Listed>
 __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t l, long long gwarp, long long nwarps,
-                                           int* dmin, int4* app_it, int* app_dx) {
+                                           int* dmin, int32_t* app_e) {
     const unsigned lane = lane_id();
     const unsigned le = lanemask_lt() | (1u << lane);
     int32_t dm = INT32_MAX;
     const int slot = r % 3, buf = r & 1;
     const int nslot = (r + 1) % 3, nbuf = buf ^ 1;
     const int wib = threadIdx.x / kWarp;
-    AppendBuf B{app_it + wib * kAppBuf, app_dx + wib * kAppBuf, 0, 0ull};
+    AppendBuf B{app_e + wib * kAppBuf, 0, 0ull};
     const unsigned long long packed = ld_cg_u64(&A.ctl->q[slot]);
     const long long N = (long long)(packed >> kCandBits);
     const long long T = (long long)(packed & kCandMask);
@@ -678,8 +731,13 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         if (wga) A.es[ga].y = r + 1;
         if (wfb) A.es[fb].y = r + 1;
         if (wgb) A.es[gb].y = r + 1;
-        warp_append2_staged<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, B, &A.ctl->fe[nslot]);
-        warp_append2_staged<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, B, &A.ctl->fe[nslot]);
+        if (Listed) {
+            warp_append2_staged<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, B, &A.ctl->fe[nslot]);
+            warp_append2_staged<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, B, &A.ctl->fe[nslot]);
+        } else {
+            warp_append2_direct<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, &A.ctl->fe[nslot]);
+            warp_append2_direct<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, &A.ctl->fe[nslot]);
+        }
         if (has_b) {
             i0 = wb.i0n;
             base0 = wb.base0n;
@@ -688,18 +746,23 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
             base0 = wa.base0n;
         }
     }
-    append_flush(A, nslot, nbuf, B, &A.ctl->fe[nslot]);
+    if (Listed) append_flush<Listed>(A, nslot, nbuf, B, &A.ctl->fe[nslot]);
     fold_min(dmin, dm);
 }
 
 #ifndef TDT_PEEL_MINB
 #define TDT_PEEL_MINB 2
 #endif
+// The search-mode sub-round (no lists) in a separate function.
+__device__ __noinline__ void process_round_search(const PeelArgs& A, int r, int32_t l, long long gwarp,
+                                                  long long nwarps, int* dmin, int32_t* app_e) {
+    process_round<false>(A, r, l, gwarp, nwarps, dmin, app_e);
+}
+
 // A is a __grid_constant__ parameter: the helpers take it by reference and
 // read its fields from the parameter bank instead of a local copy.
 __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const __grid_constant__ PeelArgs A) {
-    __shared__ int4 s_app_it[kPeelWarps * kAppBuf];  // per-warp append staging of the sub-rounds
-    __shared__ int s_app_dx[kPeelWarps * kAppBuf];
+    __shared__ int32_t s_app_e[kPeelWarps * kAppBuf];  // per-warp append staging
     const bool listed = A.lists != nullptr && *(volatile int*)&A.ctl->listed != 0;
     const int wib = threadIdx.x / kWarp;
     const int64_t gwarp = (int64_t)blockIdx.x * kPeelWarps + wib;
@@ -713,7 +776,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const _
     int ntrans = 0, np = 0;
     bool ok;
     if (A.mode == 0) {
-        ok = level_transition(A, listed, 0, ntrans++, np, &l, s_app_it, s_app_dx);
+        ok = level_transition(A, listed, 0, ntrans++, np, &l, s_app_e);
     } else {
         l = A.fixed_level;
         ok = fixed_collect(A, listed, l, 0, np);
@@ -731,8 +794,12 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const _
             if (globaltimer_ns() - t_start > A.deadline_ns) set_status(A.ctl, TDT_ERR_TIMEOUT);
         }
         // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
-        if (listed) process_round<true>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_it, s_app_dx);
-        else process_round<false>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_it, s_app_dx);
+        if (listed) process_round<true>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_e);
+#if TDT_SEARCH_NOINLINE
+        else process_round_search(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_e);
+#else
+        else process_round<false>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_e);
+#endif
         __syncthreads();
         const uint64_t t_p = globaltimer_ns();
         if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
@@ -756,7 +823,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const _
                 continue;
             }
             int32_t nl;
-            const bool more = level_transition(A, listed, r + 1, ntrans++, np, &nl, s_app_it, s_app_dx);
+            const bool more = level_transition(A, listed, r + 1, ntrans++, np, &nl, s_app_e);
             if (master) A.ctl->t_trans += globaltimer_ns() - t_b;
             if (!more) break;
             l = nl;
