@@ -137,11 +137,13 @@ __device__ __forceinline__ unsigned long long reserve_items(const PeelArgs& A, i
     return __shfl_sync(kFull, old, 0);
 }
 
-// Sub-round appends are staged per warp in shared memory and reserved in the
-// queue in batches: one queue atomic (and one frontier-count atomic) per
-// flush instead of two per warp step that marks an edge, which keeps the
-// reservation's round trip and the contention on the round's counters out of
-// most steps.  The queue order of items changes nothing: a sub-round is a set.
+// Appends of the listed sub-rounds and of the level changes are staged per
+// warp in shared memory (edge ids only, 256 bytes a warp, so the carveout
+// leaves L1 its room) and queued in batches: one queue atomic (and one
+// frontier-count atomic) per flush instead of two per warp step that marks an
+// edge, which keeps the reservation's round trip and the contention on the
+// round's counters out of most steps.  The items are built at the flush.  The
+// queue order of items changes nothing: a sub-round is a set.
 #ifndef TDT_APPEND_BUF
 #define TDT_APPEND_BUF 64
 #endif
@@ -753,12 +755,6 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
 #ifndef TDT_PEEL_MINB
 #define TDT_PEEL_MINB 2
 #endif
-// The search-mode sub-round (no lists) in a separate function.
-__device__ __noinline__ void process_round_search(const PeelArgs& A, int r, int32_t l, long long gwarp,
-                                                  long long nwarps, int* dmin, int32_t* app_e) {
-    process_round<false>(A, r, l, gwarp, nwarps, dmin, app_e);
-}
-
 // A is a __grid_constant__ parameter: the helpers take it by reference and
 // read its fields from the parameter bank instead of a local copy.
 __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const __grid_constant__ PeelArgs A) {
@@ -795,11 +791,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const _
         }
         // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
         if (listed) process_round<true>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_e);
-#if TDT_SEARCH_NOINLINE
-        else process_round_search(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_e);
-#else
         else process_round<false>(A, r, l, gwarp, nwarps, &A.ctl->dmin[(ntrans + 1) & 1], s_app_e);
-#endif
         __syncthreads();
         const uint64_t t_p = globaltimer_ns();
         if (!grid_barrier(&A.ctl->g, gridDim.x)) return;
