@@ -18,8 +18,10 @@
 // the block's warps split evenly and walk 32 entries per step (the same owner
 // reduction as the support pass).  Slots come from one 64-bit cursor per edge
 // (start of its role-C segment); every store is checked against the end of
-// the edge's list, and check_kernel verifies afterwards that every cursor
-// reached it (else TDT_ERR_CAPACITY).
+// the lists (one bound for the kernel instead of a random load of the edge's
+// own end per entry), and check_kernel verifies afterwards that every cursor
+// ended exactly at its edge's list end (else TDT_ERR_CAPACITY, and the lists
+// are not used).
 #include "common.cuh"
 
 namespace tdt {
@@ -56,6 +58,9 @@ __global__ void __launch_bounds__(kTrBlock, kTrMinBlocks) transpose_kernel(TrArg
     const unsigned le = lanemask_lt() | (1u << lane);
     const int64_t ne = A.ne;
     const long long ngroups = (ne + kTrBlock - 1) / kTrBlock;
+    // stores stay inside the lists; tr_check_kernel then requires every
+    // cursor to end exactly at its own list end
+    const unsigned long long cap = (unsigned long long)__ldg(A.off + ne);
     for (;;) {
         if (threadIdx.x == 0) s_group = (long long)atomicAdd(next, 1ull);
         __syncthreads();
@@ -134,7 +139,7 @@ __global__ void __launch_bounds__(kTrBlock, kTrMinBlocks) transpose_kernel(TrArg
                         tr_fail(A);
                     } else {
                         const unsigned long long slot = atomicAdd(A.cur + eC, 1ull);
-                        if (slot < (unsigned long long)__ldg(A.off + eC + 1)) A.lists[slot] = make_int2(s_VI[o], ent.x);
+                        if (slot < cap) A.lists[slot] = make_int2(s_VI[o], ent.x);
                         else tr_fail(A);
                     }
                 }
