@@ -8,8 +8,9 @@ outputs) of that graph.
 
 * value: edges/s with the CSR resident in HBM (inputs larger than L2);
 * e2e:   the same through truss_decompose with host buffers: each step
-         copies rows/cols/row_ptr from pinned host memory and reads the
-         per-edge truss numbers back;
+         copies the CSR (columns, row_ptr) from pinned host memory (the COO
+         rows are derived on the device) and reads the per-edge truss
+         numbers back;
 * roofline: algorithmic bytes over CUDA-event time: a decomposition moves
          B_dec = 2 B_sup (B_sup = 4W + 28E + 4(V+1), W = sum over edges of
          d+(u)+d+(v)): the support pass, then one re-enumeration of each
@@ -592,24 +593,22 @@ def main_ours(args):
     ms_step = t_ms / args.steps
     value = ws * E / (ms_step / 1e3)
 
-    # e2e: host buffers through the public API
-    rows_h = g.rows.cpu().pin_memory()
+    # e2e: host buffers through the public API.  The graph goes over as CSR
+    # (columns + row_ptr): truss_decompose derives the COO rows on the device
+    # when a CSRCOO comes without them, so they are not copied.
     cols_h = g.columns.cpu().pin_memory()
     rp_h = g.row_ptr.cpu().pin_memory()
     truss_h = torch.empty(E, dtype=torch.int32).pin_memory()
     from tdtdecomposition_gb300 import CSRCOO
-    d_rows = torch.empty_like(g.rows)
     d_cols = torch.empty_like(g.columns)
     d_rp = torch.empty_like(g.row_ptr)
 
     e2e_stats = []
 
     def e2e_step():
-        d_rows.copy_(rows_h, non_blocking=True)
         d_cols.copy_(cols_h, non_blocking=True)
         d_rp.copy_(rp_h, non_blocking=True)
-        tr, _, _, st = T.truss_decompose(CSRCOO(columns=d_cols, row_ptr=d_rp, rows=d_rows), workspace=wsp,
-                                         sync=False)
+        tr, _, _, st = T.truss_decompose(CSRCOO(columns=d_cols, row_ptr=d_rp), workspace=wsp, sync=False)
         truss_h.copy_(tr, non_blocking=True)
         e2e_stats.append(st)
 
@@ -633,7 +632,7 @@ def main_ours(args):
               file=sys.stderr, flush=True)
         raise SystemExit(3)
     e2e_value = ws * E / (te / args.steps / 1e3)
-    h2d = rows_h.numel() * 4 + cols_h.numel() * 4 + rp_h.numel() * 8
+    h2d = cols_h.numel() * 4 + rp_h.numel() * 8
     d2h = truss_h.numel() * 4
 
     if rank != 0:
