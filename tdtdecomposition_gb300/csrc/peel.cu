@@ -64,6 +64,7 @@ struct PeelCtl {
     // block 0's time (ns) in candidate processing, grid-barrier waits after
     // processing, and level transitions; diagnostic only
     unsigned long long t_proc, t_wait, t_trans, t_total;
+    unsigned long long grab[3];    // slot cursor of search-mode sub-round r, at r % 3
 };
 
 struct PeelArgs {
@@ -326,6 +327,15 @@ __device__ __forceinline__ void pass_min(const PeelArgs& A, int np, int32_t v) {
 // Level-change passes stream the alive list in steps of kStep x 32 entries per
 // warp: the gathers of a step are in flight together and the step reserves its
 // output ranges with one atomic each.
+#ifndef TDT_DYN_CHUNK
+#define TDT_DYN_CHUNK 256
+#endif
+#ifndef TDT_DYN_MIN_LOG2
+#define TDT_DYN_MIN_LOG2 20
+#endif
+constexpr long long kDynChunk = TDT_DYN_CHUNK;  // 0: static ranges in search mode too
+constexpr int kDynMinLog2 = TDT_DYN_MIN_LOG2;
+static_assert(kDynChunk % 64 == 0, "dynamic ranges are whole 64-slot steps");
 #ifndef TDT_PEEL_STEP
 #define TDT_PEEL_STEP 8
 #endif
@@ -658,11 +668,23 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     const long long T = (long long)(packed & kCandMask);
     const long long* __restrict__ qb = A.qb[buf];
     const int4* __restrict__ qi = A.qi[buf];
-    // each warp owns a contiguous range of candidate slots (a multiple of 64)
+    // listed mode: each warp owns a contiguous range of candidate slots (a
+    // multiple of 64).  Search mode with many slots: warps take ranges of
+    // kDynChunk slots from a shared cursor (the binary search of a slot costs
+    // from one load to twenty, so equal ranges finish far apart).
+    const bool dyn = !Listed && kDynChunk > 0 && T >= (1ll << kDynMinLog2);
     const long long per_warp = (((T + nwarps - 1) / nwarps) + 63) & ~63ll;
-    const long long cb0 = gwarp * per_warp;
-    const long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
-    if (cb0 >= cb1) return;
+    long long cb0 = gwarp * per_warp;
+    long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
+    if (!dyn && cb0 >= cb1) return;
+    for (;;) {
+    if (dyn) {
+        unsigned long long c = 0;
+        if (lane == 0) c = atomicAdd(&A.ctl->grab[slot], (unsigned long long)kDynChunk);
+        cb0 = (long long)__shfl_sync(kFull, c, 0);
+        if (cb0 >= T) break;
+        cb1 = cb0 + kDynChunk < T ? cb0 + kDynChunk : T;
+    }
     // item of slot cb0 = last i with qb[i] <= cb0: a 32-way search, each step
     // one load per lane (log32 N dependent loads instead of log2 N)
     long long i0 = 0;
@@ -748,6 +770,8 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
             base0 = wa.base0n;
         }
     }
+    if (!dyn) break;
+    }
     if (Listed) append_flush<Listed>(A, nslot, nbuf, B, &A.ctl->fe[nslot]);
     fold_min(dmin, dm);
 }
@@ -787,6 +811,7 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const _
             A.round_level[r] = l;
             A.ctl->q[(r + 2) % 3] = 0;
             A.ctl->fe[(r + 2) % 3] = 0;
+            A.ctl->grab[(r + 2) % 3] = 0;
             if (globaltimer_ns() - t_start > A.deadline_ns) set_status(A.ctl, TDT_ERR_TIMEOUT);
         }
         // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
