@@ -84,6 +84,12 @@ void tdt_set_peel_deadline_ns(long long ns);
  * edges outnumber the queue); lower values let small graphs run several
  * batches.  <= 0 restores a default.  Results do not depend on it. */
 void tdt_set_ktruss_batch_caps(long long items, long long cands);
+/* Testing knob of the peel without triangle lists (no counterpart in the
+ * reference): sub-rounds of at least `slots` candidate slots are split among
+ * the warps in 256-slot ranges taken from a shared cursor instead of one
+ * equal range per warp (default 2^20; lower values take the dynamic split on
+ * small graphs).  <= 0 restores the default.  Results do not depend on it. */
+void tdt_set_peel_dynamic_min(long long slots);
 int tdt_test_barrier_timeout(void *workspace, long long limit_ns, cudaStream_t stream);
 
 /* =====================================================================

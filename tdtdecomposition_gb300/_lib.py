@@ -30,6 +30,7 @@ _SIGS = [
     ("tdt_set_support_caps", None, [ctypes.c_int, ctypes.c_int]),
     ("tdt_set_peel_deadline_ns", None, [ctypes.c_longlong]),
     ("tdt_set_ktruss_batch_caps", None, [ctypes.c_longlong, ctypes.c_longlong]),
+    ("tdt_set_peel_dynamic_min", None, [ctypes.c_longlong]),
     ("tdt_test_barrier_timeout", ctypes.c_int, [c_ptr, ctypes.c_longlong, c_ptr]),
     ("tdt_segment_add", ctypes.c_int, [c_ptr, c_i64, c_ptr, c_ptr, c_i64, c_ptr]),
     ("tdt_segment_isin2", ctypes.c_int, [c_ptr, c_ptr, c_ptr, c_i64, c_ptr, c_i64, c_ptr]),

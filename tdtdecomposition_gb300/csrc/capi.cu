@@ -90,6 +90,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
 void set_support_caps(int warp_cap, int heavy_cap);
 void set_peel_deadline(long long ns);
 void set_fixed_caps(long long items, long long cands);
+void set_peel_dyn_min(long long slots);
 int test_barrier_timeout(void* ws, long long limit_ns, cudaStream_t st);
 int launch_support_accum_i32(const int32_t* rp, int32_t stride, const int32_t* cols, int64_t nv, int64_t ne,
                              int32_t* out, cudaStream_t st);
@@ -132,6 +133,7 @@ API unsigned long long tdt_launch_count(void) { return __atomic_load_n(&g_launch
 API void tdt_set_support_caps(int warp_cap, int heavy_cap) { set_support_caps(warp_cap, heavy_cap); }
 API void tdt_set_peel_deadline_ns(long long ns) { set_peel_deadline(ns); }
 API void tdt_set_ktruss_batch_caps(long long items, long long cands) { set_fixed_caps(items, cands); }
+API void tdt_set_peel_dynamic_min(long long slots) { set_peel_dyn_min(slots); }
 API int tdt_test_barrier_timeout(void* workspace, long long limit_ns, cudaStream_t stream) {
     return test_barrier_timeout(workspace, limit_ns, stream);
 }

@@ -86,6 +86,7 @@ struct PeelArgs {
     int32_t fixed_level;
     unsigned long long deadline_ns;  // wall-clock budget of the launch
     unsigned long long fixed_item_cap, fixed_cand_cap;  // k-truss collection batch limits
+    long long dyn_min_slots;      // search mode: sub-rounds of at least this many slots take dynamic ranges
     PeelCtl* ctl;
 };
 
@@ -672,7 +673,7 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     // multiple of 64).  Search mode with many slots: warps take ranges of
     // kDynChunk slots from a shared cursor (the binary search of a slot costs
     // from one load to twenty, so equal ranges finish far apart).
-    const bool dyn = !Listed && kDynChunk > 0 && T >= (1ll << kDynMinLog2);
+    const bool dyn = !Listed && kDynChunk > 0 && T >= A.dyn_min_slots;
     const long long per_warp = (((T + nwarps - 1) / nwarps) + 63) & ~63ll;
     long long cb0 = gwarp * per_warp;
     long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
@@ -1059,6 +1060,8 @@ static long long g_peel_deadline_ns = 0;
 void set_peel_deadline(long long ns) { g_peel_deadline_ns = ns; }
 
 // Test hook: lower the k-truss collection batch limits (<= 0: the defaults).
+static long long g_dyn_min_slots = 0;
+void set_peel_dyn_min(long long slots) { g_dyn_min_slots = slots; }
 static long long g_fixed_item_cap = 0, g_fixed_cand_cap = 0;
 void set_fixed_caps(long long items, long long cands) {
     g_fixed_item_cap = items;
@@ -1271,6 +1274,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     A.mode = mode == 0 ? 0 : 1;
     A.fixed_level = fixed_level;
     A.deadline_ns = g_peel_deadline_ns > 0 ? (unsigned long long)g_peel_deadline_ns : kPeelDeadlineNs;
+    A.dyn_min_slots = g_dyn_min_slots > 0 ? g_dyn_min_slots : (1ll << kDynMinLog2);
     A.fixed_item_cap = g_fixed_item_cap > 0 && (unsigned long long)g_fixed_item_cap < kFixedItemCap
                            ? (unsigned long long)g_fixed_item_cap : kFixedItemCap;
     A.fixed_cand_cap = g_fixed_cand_cap > 0 && (unsigned long long)g_fixed_cand_cap < kFixedCandCap

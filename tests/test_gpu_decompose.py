@@ -6,7 +6,7 @@ import torch
 
 from oracle import oracle as O
 from tests import _golden as GD
-from tdtdecomposition_gb300 import CSRCOO, generators as G, truss as T
+from tdtdecomposition_gb300 import CSRCOO, _lib, generators as G, truss as T
 from tdtdecomposition_gb300._lib import TdtError
 
 pytestmark = pytest.mark.gpu
@@ -267,3 +267,26 @@ def test_ktruss_search_in_small_batches(caps, lists):
             assert np.array_equal(m, truss >= k), (caps, k)
     finally:
         L.tdt_set_ktruss_batch_caps(0, 0)
+
+
+@pytest.mark.parametrize("scale", [12, 15])
+def test_search_peel_dynamic_ranges(scale):
+    """The peel without lists, with every sub-round split into dynamic 256-slot
+    ranges (the default only splits sub-rounds of 2^20+ slots): the same truss
+    numbers and peel order as the listed peel and the static split."""
+    s, d = G.rmat_edges(scale, 16 << scale, seed=3)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
+    g = graph_of(rows, cols, rp)
+    L = _lib.load()
+    ref = T.truss_decompose(g, lists=True)
+    static = T.truss_decompose(g, lists=False)
+    L.tdt_set_peel_dynamic_min(64)
+    try:
+        dyn = T.truss_decompose(g, lists=False)
+        kt = T.ktruss_search(g, max(3, ref.kmax // 2), lists=False)
+    finally:
+        L.tdt_set_peel_dynamic_min(0)
+    assert not dyn.listed and ref.listed
+    for r in (static, dyn):
+        assert r.kmax == ref.kmax and torch.equal(r.truss, ref.truss) and torch.equal(r.e_truss, ref.e_truss)
+    assert torch.equal(kt, ref.truss >= max(3, ref.kmax // 2))
