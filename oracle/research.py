@@ -234,3 +234,130 @@ def undirected_truss_undirect(rows, cols, directed_ptr, columns_g, edges_id_nbr,
                 row_ptr=g["pg"], columns_g=g["cg"], edges_id_nbr=g["nbr"])
 
     return _peel_loop(support, edges, lambda: len(g["cols"]), peel, compact, compact_threshold)
+
+
+# ---------------------------------------------------------------- tensor_original driver
+def symmetric_csr(rows, cols, num_v):
+    """Both directions of every edge, rows sorted by column: the CSRGraph the
+    tensor_original driver reads (vertex ids as given)."""
+    r = np.concatenate([rows, cols]).astype(np.int64)
+    c = np.concatenate([cols, rows]).astype(np.int64)
+    order = np.lexsort((c, r))
+    r, c = r[order], c[order]
+    rp = np.concatenate([[0], np.cumsum(np.bincount(r, minlength=num_v))]).astype(np.int32)
+    return rp, c.astype(np.int32)
+
+
+def _selection(starts, ends):
+    """batched_csr_selection_opt2 (helper.py:102-121) on non-empty ranges:
+    flat positions and int32 offsets."""
+    sizes = (ends - starts).astype(np.int64)
+    ptr = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    idx = np.concatenate([np.arange(a, b) for a, b in zip(starts, ends)]) if len(starts) else np.zeros(0, np.int64)
+    return idx.astype(np.int64), ptr
+
+
+def truss_tensor_original(row_ptr, columns, compact_threshold=100000):
+    """demo_truss/tensor_original/truss_nosavetri_tensor4.py:27-196
+    (truss_deposs) over a symmetric CSR: returns (e_truss, ptr_truss) over the
+    undirected edges u < v in CSR order.  As in the reference, the edges of
+    the last sub-round are not appended to e_truss (:147-152 stops first)."""
+    row_ptr = _i32(row_ptr).astype(np.int64)
+    columns = _i32(columns).copy()
+    V = len(row_ptr) - 1
+    row_indice_g = np.repeat(np.arange(V, dtype=np.int32), np.diff(row_ptr))
+    mask = row_indice_g < columns
+    row_indice = row_indice_g[mask]
+    cols_u = columns[mask]
+    Eu = len(cols_u)
+    e_truss, ptr_truss = [], [0]
+    e_mask = np.ones(Eu, bool)
+    edges_id = np.arange(Eu, dtype=np.int32)
+    edges_id_nbr = np.arange(len(columns), dtype=np.int32)
+    edges_id_nbr[mask] = edges_id
+    sorted_indices = np.argsort(columns[~mask], kind="stable")
+    temp = np.zeros(Eu, np.int32)
+    temp[sorted_indices] = edges_id
+    edges_id_nbr[~mask] = temp
+    direc = np.zeros(V, np.int32)
+    O.segment_add(mask.astype(np.int32), row_ptr.astype(np.int32), direc)
+    direc_rp = np.concatenate([[0], np.cumsum(direc)]).astype(np.int32)
+    support = np.zeros(Eu, np.int32)
+    O.segment_isin2tile(row_indice, cols_u, direc_rp, 1, support)
+    e_mask[edges_id[support == 0]] = False
+    if not e_mask.any():
+        return np.zeros(0, np.int32), np.array(ptr_truss, np.int32)
+    keep = e_mask[edges_id_nbr]
+    edges_id_nbr = edges_id_nbr[keep]
+    columns = columns[keep]
+    sizes = np.zeros(V, np.int32)
+    O.segment_add(keep.astype(np.int32), row_ptr.astype(np.int32), sizes)
+    row_ptr = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    l = 1
+    e_curr = edges_id[support == l]
+    while len(e_curr) == 0:
+        ptr_truss.append(sum(len(x) for x in e_truss))
+        l += 1
+        e_curr = edges_id[support == l]
+    e_del = 0
+    columns = np.concatenate([columns, [-1]]).astype(np.int32)
+    n_out = lambda: sum(len(x) for x in e_truss)
+    while True:
+        e_truss.append(edges_id[e_curr])
+        left, s_ptr = _selection(row_ptr[row_indice[e_curr]], row_ptr[row_indice[e_curr] + 1])
+        right, e_ptr = _selection(row_ptr[cols_u[e_curr]], row_ptr[cols_u[e_curr] + 1])
+        m1 = e_mask[edges_id_nbr[left]]
+        m2 = e_mask[edges_id_nbr[right]]
+        left = left.copy()
+        right = right.copy()
+        left[~m1] = -1
+        right[~m2] = -1
+        mk1 = np.zeros(len(left), np.uint8)
+        mk2 = np.zeros(len(right), np.uint8)
+        segment_isinis_m(columns[left], s_ptr, columns[right], e_ptr, mk1, mk2)
+        mk1, mk2 = mk1.astype(bool), mk2.astype(bool)
+        left_nbr = edges_id_nbr[left[mk1]]
+        right_nbr = edges_id_nbr[right[mk2]]
+        if len(left_nbr) == 0 or len(right_nbr) == 0:
+            e_mask[e_curr] = False
+            e_curr = left_nbr
+        else:
+            values = np.zeros(len(e_ptr) - 1, np.int32)
+            O.segment_add(mk2.astype(np.int32), e_ptr, values)
+            e_curr_rep = np.repeat(e_curr, values)
+            s1 = (support[left_nbr] > l).astype(np.uint8)
+            s2 = (support[right_nbr] > l).astype(np.uint8)
+            affect = np.zeros(len(e_mask), np.uint8)
+            sub_suppport_affect(left_nbr, right_nbr, e_curr_rep, support, s1, s2, affect, l)
+            e_del += len(e_curr)
+            e_mask[e_curr] = False
+            e_aff = np.nonzero(affect)[0]
+            e_curr = e_aff[support[e_aff] <= l].astype(np.int32)
+        if int(e_mask.sum()) == len(e_curr):
+            ptr_truss.append(n_out())
+            break
+        if e_del >= compact_threshold:
+            keep = e_mask[edges_id_nbr]
+            edges_id_nbr = edges_id_nbr[keep]
+            columns = np.concatenate([columns[:-1][keep], [-1]]).astype(np.int32)
+            sizes = np.zeros(V, np.int32)
+            O.segment_add(keep.astype(np.int32), row_ptr.astype(np.int32), sizes)
+            row_ptr = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+            e_del = 0
+            idx = np.nonzero(e_mask)[0]
+            edges_id, support, cols_u, row_indice = edges_id[idx], support[idx], cols_u[idx], row_indice[idx]
+            remap = np.zeros(len(e_mask), np.int32)
+            remap[idx] = np.arange(len(idx), dtype=np.int32)
+            e_curr = remap[e_curr]
+            edges_id_nbr = remap[edges_id_nbr]
+            e_mask = np.ones(len(idx), bool)
+        if len(e_curr) == 0:
+            ptr_truss.append(n_out())
+            l += 1
+            e_curr = np.nonzero(support == l)[0].astype(np.int32)
+            while len(e_curr) == 0:
+                ptr_truss.append(n_out())
+                l += 1
+                e_curr = np.nonzero(support == l)[0].astype(np.int32)
+    e = np.concatenate(e_truss).astype(np.int32) if e_truss else np.zeros(0, np.int32)
+    return e, np.array(ptr_truss, np.int32)

@@ -507,3 +507,135 @@ def undirected_truss_undirect(graph, columns_g, edges_id_nbr, directed_ptr, row_
                                 in_curr, l)
 
     return _undirected_peel(support, edges, lambda: g["cols"].shape[0], peel, compact, compact_threshold)
+
+
+# ------------------------------------------------------------------ tensor_original driver
+def symmetric_csr(graph):
+    """Both directions of every edge of `graph` (rows sorted by column): the
+    CSRGraph the tensor_original driver reads.  Returns (row_ptr int32,
+    columns int32)."""
+    V = graph.num_vertices
+    r = torch.cat([graph.rows, graph.columns]).to(torch.int64)
+    c = torch.cat([graph.columns, graph.rows]).to(torch.int64)
+    key = r * (V + 1) + c
+    order = torch.argsort(key)
+    r, c = r[order], c[order]
+    rp = torch.zeros(V + 1, dtype=torch.int32, device=c.device)
+    rp[1:] = torch.cumsum(torch.bincount(r, minlength=V), 0).to(torch.int32)
+    return rp, c.to(torch.int32)
+
+
+def _selection_opt2(starts, ends):
+    """batched_csr_selection_opt2 (helper.py:102-121) on non-empty ranges."""
+    return _csr_selection_ptr(starts, ends)
+
+
+def truss_tensor_original(row_ptr, columns, compact_threshold=100000):
+    """demo_truss/tensor_original/truss_nosavetri_tensor4.py:27-196
+    (truss_deposs) over a symmetric CSR (row_ptr, columns int32 on the GPU),
+    written against segment_isin2, segment_isinis_m and sub_suppport_affect:
+    returns (e_truss, ptr_truss) over the undirected edges u < v in CSR order.
+    As in the reference, the edges of the last sub-round are not appended to
+    e_truss (the loop stops first, :147-152)."""
+    dev = columns.device
+    V = row_ptr.shape[0] - 1
+    row_ptr = row_ptr.to(torch.int64)
+    columns = columns.to(torch.int32)
+    row_indice_g = torch.repeat_interleave(torch.arange(V, dtype=torch.int32, device=dev), row_ptr[1:] - row_ptr[:-1])
+    mask = row_indice_g < columns
+    row_indice = row_indice_g[mask]
+    cols_u = columns[mask]
+    Eu = cols_u.shape[0]
+    e_truss, ptr_truss = [], [0]
+    e_mask = torch.ones(Eu, dtype=torch.bool, device=dev)
+    edges_id = torch.arange(Eu, dtype=torch.int32, device=dev)
+    edges_id_nbr = torch.arange(columns.shape[0], dtype=torch.int32, device=dev)
+    edges_id_nbr[mask] = edges_id
+    sorted_indices = torch.argsort(columns[~mask], stable=True)
+    temp = torch.zeros(Eu, dtype=torch.int32, device=dev)
+    temp[sorted_indices] = edges_id
+    edges_id_nbr[~mask] = temp
+    rp32 = row_ptr.to(torch.int32)
+    direc = torch.zeros(V, dtype=torch.int32, device=dev)
+    tt.segment_add(mask.int(), rp32, direc)
+    direc_rp = torch.cat([torch.zeros(1, dtype=torch.int32, device=dev), direc.cumsum(0, dtype=torch.int32)])
+    support = torch.zeros(Eu, dtype=torch.int32, device=dev)
+    tt.segment_isin2(row_indice, cols_u, direc_rp, support)
+    e_mask[edges_id[support == 0].long()] = False
+    if not bool(e_mask.any()):
+        return torch.zeros(0, dtype=torch.int32, device=dev), torch.tensor(ptr_truss, dtype=torch.int32)
+    keep = e_mask[edges_id_nbr.long()]
+    edges_id_nbr = edges_id_nbr[keep]
+    columns = columns[keep]
+    row_ptr = update_row_ptr(keep, rp32).to(torch.int64)
+    n_out = [0]
+
+    def level_edges(l):
+        return torch.where(support == l)[0].to(torch.int32)
+
+    l = 1
+    e_curr = level_edges(l)
+    while e_curr.shape[0] == 0:
+        ptr_truss.append(n_out[0])
+        l += 1
+        e_curr = level_edges(l)
+    e_del = 0
+    columns = torch.cat([columns, torch.full((1,), -1, dtype=torch.int32, device=dev)])
+    while True:
+        e_truss.append(edges_id[e_curr.long()])
+        n_out[0] += e_curr.shape[0]
+        ec = e_curr.long()
+        left, s_ptr = _selection_opt2(row_ptr[row_indice[ec].long()], row_ptr[row_indice[ec].long() + 1])
+        right, e_ptr = _selection_opt2(row_ptr[cols_u[ec].long()], row_ptr[cols_u[ec].long() + 1])
+        m1 = e_mask[edges_id_nbr[left].long()]
+        m2 = e_mask[edges_id_nbr[right].long()]
+        left = left.clone()
+        right = right.clone()
+        left[~m1] = -1
+        right[~m2] = -1
+        mk1 = torch.zeros(left.shape[0], dtype=torch.bool, device=dev)
+        mk2 = torch.zeros(right.shape[0], dtype=torch.bool, device=dev)
+        tt.segment_isinis_m(columns[left], s_ptr, columns[right], e_ptr, mk1, mk2)
+        left_nbr = edges_id_nbr[left[mk1]]
+        right_nbr = edges_id_nbr[right[mk2]]
+        if left_nbr.shape[0] == 0 or right_nbr.shape[0] == 0:
+            e_mask[ec] = False
+            e_curr = left_nbr
+        else:
+            values = torch.zeros(e_ptr.shape[0] - 1, dtype=torch.int32, device=dev)
+            tt.segment_add(mk2.int(), e_ptr, values)
+            e_curr_rep = torch.repeat_interleave(e_curr, values.long())
+            s1 = support[left_nbr.long()] > l
+            s2 = support[right_nbr.long()] > l
+            affect = torch.zeros(e_mask.shape[0], dtype=torch.bool, device=dev)
+            tt.sub_suppport_affect(left_nbr, right_nbr, e_curr_rep, support, s1, s2, affect, l)
+            e_del += e_curr.shape[0]
+            e_mask[ec] = False
+            e_aff = torch.where(affect)[0]
+            e_curr = e_aff[support[e_aff] <= l].to(torch.int32)
+        if int(e_mask.sum()) == e_curr.shape[0]:
+            ptr_truss.append(n_out[0])
+            break
+        if e_del >= compact_threshold:
+            keep = e_mask[edges_id_nbr.long()]
+            edges_id_nbr = edges_id_nbr[keep]
+            columns = torch.cat([columns[:-1][keep], torch.full((1,), -1, dtype=torch.int32, device=dev)])
+            row_ptr = update_row_ptr(keep, row_ptr.to(torch.int32)).to(torch.int64)
+            e_del = 0
+            idx = torch.where(e_mask)[0]
+            edges_id, support, cols_u, row_indice = edges_id[idx], support[idx], cols_u[idx], row_indice[idx]
+            remap = torch.zeros(e_mask.shape[0], dtype=torch.int32, device=dev)
+            remap[idx] = torch.arange(idx.shape[0], dtype=torch.int32, device=dev)
+            e_curr = remap[e_curr.long()]
+            edges_id_nbr = remap[edges_id_nbr.long()]
+            e_mask = torch.ones(idx.shape[0], dtype=torch.bool, device=dev)
+        if e_curr.shape[0] == 0:
+            ptr_truss.append(n_out[0])
+            l += 1
+            e_curr = level_edges(l)
+            while e_curr.shape[0] == 0:
+                ptr_truss.append(n_out[0])
+                l += 1
+                e_curr = level_edges(l)
+    e = torch.cat(e_truss) if e_truss else torch.zeros(0, dtype=torch.int32, device=dev)
+    return e, torch.tensor(ptr_truss, dtype=torch.int32)

@@ -438,3 +438,58 @@ def test_unfused_support_matches_fused_on_rmat_gpu():
     a = flow.support_computing(_cu(rows), _cu(cols), rp32, 1)
     b = flow.support_computing_before(_cu(rows), _cu(cols), rp32, 1)
     assert torch.equal(a, b) and int(a.sum()) > 0
+
+
+# ------------------------------------------------------------------ tensor_original driver
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("thr", [100000, 40])
+def test_oracle_tensor_original_reproduces_reference_levels(name, thr):
+    """truss_nosavetri_tensor4.py's driver (segment_isinis_m + sub_suppport_affect)
+    peels the reference's recorded sub-rounds in order; as written there, the
+    edges of its last sub-round never reach e_truss."""
+    d, rows, cols, rp, nv = _ref_graph(name)
+    srp, sc = R.symmetric_csr(rows, cols, nv)
+    e, p = R.truss_tensor_original(srp, sc, thr)
+    want_e, want_p = d["sg_e_truss1"], d["sg_ptr_truss1"]
+    assert len(p) == len(want_p) and np.array_equal(p[:-1], want_p[:-1])
+    assert p[-1] == len(e) and np.array_equal(e, want_e[:len(e)])
+
+
+def _tensor_original_ops():
+    def support(rows, cols, rp, out):
+        O.segment_isin2tile(_np(rows), _np(cols), _np(rp), 1, _np(out))
+
+    return types.SimpleNamespace(
+        segment_add=lambda c, p, o: O.segment_add(_np(c), _np(p), _np(o)),
+        segment_isin2=support,
+        segment_isinis_m=lambda a, ap, b, bp, m1, m2: R.segment_isinis_m(_np(a), _np(ap), _np(b), _np(bp), _np(m1),
+                                                                         _np(m2)),
+        sub_suppport_affect=lambda ln, rn, cr, s, m1, m2, af, l: R.sub_suppport_affect(
+            _np(ln), _np(rn), _np(cr), _np(s), _np(m1), _np(m2), _np(af), l))
+
+
+@pytest.mark.parametrize("thr", [100000, 300])
+def test_flow_tensor_original_follows_the_oracle_steps(monkeypatch, thr):
+    monkeypatch.setattr(flow, "tt", _tensor_original_ops())
+    s, t = G.rmat_edges(10, 16 << 10, seed=6)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, t], 1))
+    nv = len(verts)
+    g = CSRCOO(columns=torch.as_tensor(cols, dtype=torch.int32), row_ptr=torch.as_tensor(rp, dtype=torch.int64),
+               rows=torch.as_tensor(rows, dtype=torch.int32))
+    srp, sc = flow.symmetric_csr(g)
+    o_rp, o_c = R.symmetric_csr(rows, cols, nv)
+    assert np.array_equal(srp.numpy(), o_rp) and np.array_equal(sc.numpy(), o_c)
+    e, p = flow.truss_tensor_original(srp, sc, thr)
+    we, wp = R.truss_tensor_original(o_rp, o_c, thr)
+    assert np.array_equal(e.numpy(), we) and np.array_equal(p.numpy(), wp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_flow_tensor_original_gpu(name):
+    d, rows, cols, rp, nv = _ref_graph(name)
+    g = CSRCOO(columns=_cu(cols), row_ptr=_cu(rp, torch.int64), rows=_cu(rows))
+    srp, sc = flow.symmetric_csr(g)
+    e, p = flow.truss_tensor_original(srp, sc, compact_threshold=200)
+    we, wp = R.truss_tensor_original(*R.symmetric_csr(rows, cols, nv), 200)
+    assert np.array_equal(_host(e), we) and np.array_equal(p.numpy(), wp)
