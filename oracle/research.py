@@ -6,11 +6,14 @@ operators and the drivers that use them.
 * numpy restatements of the undirected-graph drivers
   ``demo_truss/undirected/truss_undirect_cuda.py`` (symmetric adjacency,
   ``peeling_undirect``) and ``truss_undirect_cuda2.py`` (out- and in-lists,
-  ``peeling_direct_oo/ii/oi``), step by step.
+  ``peeling_direct_oo/ii/oi``), and of the pure-tensor driver
+  ``demo_truss/tensor_original/truss_nosavetri_tensor4.py``
+  (``segment_isinis_m`` + ``sub_suppport_affect``), step by step.
 
 The reference's OpenMP file has no twin of these operators, so the pin is
-semantic: the drivers' per-edge truss numbers must equal those of the pinned
-``k_truss`` oracle.  Only tests/ may import this module.
+through the drivers: each reproduces the sub-rounds the reference's own
+``--cuda`` flow recorded for the golden graphs (tests/test_research_ops.py).
+Only tests/ may import this module.
 """
 import ctypes
 
