@@ -337,6 +337,14 @@ __device__ __forceinline__ void pass_min(const PeelArgs& A, int np, int32_t v) {
 constexpr long long kDynChunk = TDT_DYN_CHUNK;  // 0: static ranges in search mode too
 constexpr int kDynMinLog2 = TDT_DYN_MIN_LOG2;
 static_assert(kDynChunk % 64 == 0, "dynamic ranges are whole 64-slot steps");
+// An edge already marked for sub-round r+1 (support <= l) is not decremented
+// again: its support no longer decides anything (it is peeled next sub-round,
+// and its truss number is the level).
+#ifndef TDT_SKIP_MARKED
+#define TDT_SKIP_MARKED 1
+#endif
+constexpr bool kSkipMarked = TDT_SKIP_MARKED != 0;
+
 #ifndef TDT_PEEL_STEP
 #define TDT_PEEL_STEP 8
 #endif
@@ -732,13 +740,13 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         bool dfa = false, dga = false, dfb = false, dgb = false;
         if (tra && (rfa == -1 || rfa >= r) && (rga == -1 || rga >= r)) {
             const bool ff = rfa == r, fg = rga == r;
-            dfa = !ff && (!fg || ita.x < ga);
-            dga = !fg && (!ff || ita.x < fa);
+            dfa = !ff && (!fg || ita.x < ga) && (!kSkipMarked || rfa != r + 1);
+            dga = !fg && (!ff || ita.x < fa) && (!kSkipMarked || rga != r + 1);
         }
         if (trb && (rfb == -1 || rfb >= r) && (rgb == -1 || rgb >= r)) {
             const bool ff = rfb == r, fg = rgb == r;
-            dfb = !ff && (!fg || itb.x < gb);
-            dgb = !fg && (!ff || itb.x < fb);
+            dfb = !ff && (!fg || itb.x < gb) && (!kSkipMarked || rfb != r + 1);
+            dgb = !fg && (!ff || itb.x < fb) && (!kSkipMarked || rgb != r + 1);
         }
         // issue all decrements before using any result
         int32_t ofa = 0, oga = 0, ofb = 0, ogb = 0;
