@@ -88,8 +88,9 @@ def rmat_edges_device(scale, m, a=0.57, b=0.19, c=0.19, seed=1, device="cuda"):
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
                    ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-    _lib.check(fn(scale, m, seed, ta, tab, tabc, src.data_ptr(), dst.data_ptr(),
-                  torch.cuda.current_stream().cuda_stream), "tdt_gen_rmat")
+    with torch.cuda.device(src.device):
+        _lib.check(fn(scale, m, seed, ta, tab, tabc, src.data_ptr(), dst.data_ptr(),
+                      torch.cuda.current_stream(src.device).cuda_stream), "tdt_gen_rmat")
     return src, dst
 
 
@@ -137,8 +138,9 @@ def chung_lu_edges_device(n, gamma=2.1, mean_degree=40.0, max_degree=1 << 20, se
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-    _lib.check(fn(n, m, seed, cum_d.data_ptr(), total, src.data_ptr(), dst.data_ptr(),
-                  torch.cuda.current_stream().cuda_stream), "tdt_gen_chung_lu")
+    with torch.cuda.device(src.device):
+        _lib.check(fn(n, m, seed, cum_d.data_ptr(), total, src.data_ptr(), dst.data_ptr(),
+                      torch.cuda.current_stream(src.device).cuda_stream), "tdt_gen_chung_lu")
     del cum_d
     return src, dst
 

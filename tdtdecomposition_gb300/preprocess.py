@@ -50,10 +50,11 @@ def preprocess_edges(src, dst, vertex_group=None, num_ids=None, workspace=None):
     need = L.tdt_preprocess_workspace_bytes(m, num_ids)
     ws = (workspace.get(need) if workspace is not None
           else torch.empty(need, dtype=torch.uint8, device=dev))
-    rc = L.tdt_preprocess(src.data_ptr(), dst.data_ptr(), m, num_ids,
-                          vertex_group.data_ptr() if vertex_group is not None else None, ng,
-                          rows.data_ptr(), cols.data_ptr(), rp.data_ptr(), verts.data_ptr(), counts.data_ptr(),
-                          ws.data_ptr(), ws.numel(), torch.cuda.current_stream(dev).cuda_stream)
+    with torch.cuda.device(dev):
+        rc = L.tdt_preprocess(src.data_ptr(), dst.data_ptr(), m, num_ids,
+                              vertex_group.data_ptr() if vertex_group is not None else None, ng,
+                              rows.data_ptr(), cols.data_ptr(), rp.data_ptr(), verts.data_ptr(), counts.data_ptr(),
+                              ws.data_ptr(), ws.numel(), torch.cuda.current_stream(dev).cuda_stream)
     _lib.check(rc, "tdt_preprocess")
     E, V, st = (int(x) for x in counts.cpu())
     if st != 0:

@@ -132,9 +132,10 @@ def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto",
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
     # pass the requested size, not the (possibly larger, shared) buffer: the
     # device keeps lists exactly when the tail it is given holds them
-    rc = L.tdt_truss_decompose(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
-                               truss.data_ptr(), e_truss.data_ptr(), ptr.data_ptr(), cap, stats.data_ptr(),
-                               ws.data_ptr(), base + tail, s)
+    with torch.cuda.device(cols.device):
+        rc = L.tdt_truss_decompose(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
+                                   truss.data_ptr(), e_truss.data_ptr(), ptr.data_ptr(), cap, stats.data_ptr(),
+                                   ws.data_ptr(), base + tail, s)
     _lib.check(rc, "tdt_truss_decompose")
     if not sync:
         return truss, e_truss, ptr, stats
@@ -158,8 +159,9 @@ def ktruss_search(graph, k, workspace=None, stream=None, lists="auto"):
     tail = _list_bytes(wso, cols, rp, lists, base)
     ws = wso.get(base + tail)
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
-    rc = L.tdt_ktruss_search(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
-                             int(k), mask.data_ptr(), stats.data_ptr(), ws.data_ptr(), base + tail, s)
+    with torch.cuda.device(cols.device):
+        rc = L.tdt_ktruss_search(rows.data_ptr() if rows is not None else None, cols.data_ptr(), rp.data_ptr(), V, E,
+                                 int(k), mask.data_ptr(), stats.data_ptr(), ws.data_ptr(), base + tail, s)
     _lib.check(rc, "tdt_ktruss_search")
     _check_stats(stats.cpu(), "tdt_ktruss_search")
     return mask
@@ -170,8 +172,9 @@ def triangle_count_arrays(cols, rp, ws):
     V, E = rp.shape[0] - 1, cols.shape[0]
     stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=cols.device)
     buf = ws.get(L.tdt_decompose_workspace_bytes(V, E))
-    rc = L.tdt_triangle_count(cols.data_ptr(), rp.data_ptr(), V, E, None, stats.data_ptr(), buf.data_ptr(),
-                              buf.numel(), torch.cuda.current_stream(cols.device).cuda_stream)
+    with torch.cuda.device(cols.device):
+        rc = L.tdt_triangle_count(cols.data_ptr(), rp.data_ptr(), V, E, None, stats.data_ptr(), buf.data_ptr(),
+                                  buf.numel(), torch.cuda.current_stream(cols.device).cuda_stream)
     _lib.check(rc, "tdt_triangle_count")
     sh = stats.cpu()
     _check_stats(sh, "tdt_triangle_count")
@@ -188,8 +191,10 @@ def triangle_count(graph, workspace=None, stream=None, return_support=False):
     stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
     ws = _ws_for(dev, workspace).get(L.tdt_decompose_workspace_bytes(V, E))
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
-    rc = L.tdt_triangle_count(cols.data_ptr(), rp.data_ptr(), V, E, support.data_ptr() if support is not None else None,
-                              stats.data_ptr(), ws.data_ptr(), ws.numel(), s)
+    with torch.cuda.device(cols.device):
+        rc = L.tdt_triangle_count(cols.data_ptr(), rp.data_ptr(), V, E,
+                                  support.data_ptr() if support is not None else None,
+                                  stats.data_ptr(), ws.data_ptr(), ws.numel(), s)
     _lib.check(rc, "tdt_triangle_count")
     sh = stats.cpu()
     _check_stats(sh, "tdt_triangle_count")

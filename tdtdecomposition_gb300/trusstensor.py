@@ -66,6 +66,11 @@ def _same_device(*ts):
     for t in ts[1:]:
         if t.device != d:
             raise ValueError("all tensors must be on the same device (%s vs %s)" % (d, t.device))
+    # the operators launch on the current device and its current stream, as
+    # the reference's do; tensors of another device would be handed to it
+    if d.type == "cuda" and d.index is not None and d.index != torch.cuda.current_device():
+        raise ValueError("tensors are on %s but the current device is cuda:%d (use torch.cuda.device)"
+                         % (d, torch.cuda.current_device()))
     return d
 
 
