@@ -43,7 +43,7 @@ constexpr int kSupBlock = 512;                 // 16 warps
 constexpr int kSupWarps = kSupBlock / kWarp;
 constexpr int kSupMinBlocks = 3;               // resident blocks per SM (registers <= 42)
 constexpr int kSupSmemBytes = 64 * 1024;       // dynamic shared memory per block
-constexpr int kVertexBatch = 8;                // light vertices per dynamic grab
+constexpr int kVertexBatch = 2;                // light vertices per grab below the top quarter of ids
 constexpr int kHeavyChunk = 16;                // vertices scanned per heavy grab
 constexpr int kQueue = 64;                     // candidate queue entries per warp
 
@@ -499,16 +499,23 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
     Q.n = 0;
     const long long gw = (long long)blockIdx.x * kSupWarps + wib;
     const long long nw = (long long)gridDim.x * kSupWarps;
+    // rows are taken from the top id down: the top quarter of the ids (the
+    // rows whose out-neighbours have the longest lists) one row per grab, the
+    // rest kVertexBatch rows per grab, so no warp is left with a long batch
+    // while the others idle
+    const unsigned long long t1 = ((unsigned long long)nv + 3) / 4;
     for (long long it = 0;; it++) {
-        unsigned long long b = 0;
+        unsigned long long t = 0;
         if (ctl) {
-            if (lane == 0) b = atomicAdd(&ctl->light_next, (unsigned long long)kVertexBatch);
-            b = __shfl_sync(kFull, b, 0);
+            if (lane == 0) t = atomicAdd(&ctl->light_next, 1ull);
+            t = __shfl_sync(kFull, t, 0);
         } else {
-            b = (unsigned long long)((gw + it * nw) * kVertexBatch);
+            t = (unsigned long long)(gw + it * nw);
         }
+        const unsigned long long b = t < t1 ? t : t1 + (t - t1) * kVertexBatch;
+        const int nq = t < t1 ? 1 : kVertexBatch;
         if ((long long)b >= nv) break;
-        for (int q = 0; q < kVertexBatch; q++) {
+        for (int q = 0; q < nq; q++) {
             const long long uu = nv - 1 - ((long long)b + q);
             if (uu < 0) break;
             const Off bu = G.begin(uu);
