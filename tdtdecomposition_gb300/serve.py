@@ -68,8 +68,13 @@ def answer_for(query, truss_slice):
     return truss_slice >= int(query[1])
 
 
+# Workspace tail for triangle lists: the device keeps lists for a batch when
+# its 24 T bytes fit, else it runs the search peel (no counting pass first).
+DEFAULT_LIST_BUDGET = 24e9
+
+
 class TrussServer:
-    def __init__(self, device=None, memory_budget=150e9, max_batch_edges=1 << 28, list_budget=24e9):
+    def __init__(self, device=None, memory_budget=150e9, max_batch_edges=1 << 28, list_budget=DEFAULT_LIST_BUDGET):
         dev = torch.device(device) if device is not None else torch.device("cuda")
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
