@@ -121,58 +121,76 @@ __device__ __forceinline__ Off find_sorted(const int32_t* __restrict__ cols, Off
 
 // ------------------------------------------------------------------ grid barrier
 // Control block shared by the persistent kernels (device memory, zeroed by the
-// host before a launch).
-// The arrival counter and the generation word sit in separate 128-byte lines
-// so the blocks polling the generation do not queue in front of arrivals.
+// host before a launch).  One 64-bit arrival counter that only grows: barrier
+// k of a launch is complete when it reaches k x nblocks, so the last block to
+// arrive releases the others with its own increment (no reset, no second
+// word to publish).  Bit 63 of the same word aborts the run: a waiter sees it
+// in the value it polls and an arriving block in the value its increment
+// returns, with no extra load on the barrier's path.
 struct GridCtl {
-    unsigned bar_count;
-    unsigned pad0[31];
-    unsigned bar_gen;
-    unsigned pad1[31];
-    int abort;
+    unsigned long long arrive;
+    unsigned pad0[62];
+    int pad1;
     int status;
     unsigned pad2[30];
 };
+static_assert(sizeof(GridCtl) == 384, "control block layout");
+
+constexpr unsigned long long kGridAbortBit = 1ull << 63;
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Makes every block leave at its next grid barrier (and any block waiting at
+// one now).
+__device__ __forceinline__ void grid_abort(GridCtl* ctl) { atomicOr(&ctl->arrive, kGridAbortBit); }
 
 // Wait limit of one grid barrier.  A barrier that does not complete within it
 // sets GridCtl::status = TDT_ERR_TIMEOUT and every block leaves its loop.
 constexpr uint64_t kBarrierTimeoutNs = 20ull * 1000ull * 1000ull * 1000ull;
 
-// Sense-free generation barrier over all blocks of a cooperative launch.
-// Returns false when the run is being aborted (timeout or an error elsewhere).
+// Barrier over all blocks of a cooperative launch.  Returns false when the
+// run is being aborted (timeout or an error elsewhere).
 __device__ __forceinline__ bool grid_barrier(GridCtl* ctl, unsigned nblocks,
                                              uint64_t limit_ns = kBarrierTimeoutNs) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        unsigned gen = ld_acquire_u32(&ctl->bar_gen);
-        __threadfence();
-        unsigned prev = atomicAdd(&ctl->bar_count, 1u);
-        if (prev == nblocks - 1) {
-            atomicExch(&ctl->bar_count, 0u);
-            __threadfence();
-            atomicAdd(&ctl->bar_gen, 1u);
+        __threadfence();  // the block's writes before its arrival
+        const unsigned long long old = atomicAdd(&ctl->arrive, 1ull);
+        if (old & kGridAbortBit) {
+            ok = 0;
         } else {
-            // one load per spin; the abort flag and the clock every 32 spins,
-            // and a short sleep once the wait is long
-            uint64_t t0 = globaltimer_ns();
-            unsigned spins = 0;
-            while (ld_acquire_u32(&ctl->bar_gen) == gen) {
-                if ((++spins & 31u) == 0) {
-                    if (ld_volatile_i32(&ctl->abort)) { ok = 0; break; }
-                    if (globaltimer_ns() - t0 > limit_ns) {
-                        atomicMax(&ctl->status, (int)TDT_ERR_TIMEOUT);
-                        atomicExch(&ctl->abort, 1);
+            const unsigned long long target = (old / nblocks + 1) * nblocks;
+            if (old + 1 != target) {
+                // one load per spin; the clock every 32 spins, and a short
+                // sleep once the wait is long
+                const uint64_t t0 = globaltimer_ns();
+                unsigned spins = 0;
+                for (;;) {
+                    const unsigned long long v = ld_acquire_u64(&ctl->arrive);
+                    if (v & kGridAbortBit) {
                         ok = 0;
                         break;
                     }
-                    if (spins > 4096) __nanosleep(200);
+                    if (v >= target) break;
+                    if ((++spins & 31u) == 0) {
+                        if (globaltimer_ns() - t0 > limit_ns) {
+                            atomicMax(&ctl->status, (int)TDT_ERR_TIMEOUT);
+                            grid_abort(ctl);
+                            ok = 0;
+                            break;
+                        }
+                        if (spins > 4096) __nanosleep(200);
+                    }
                 }
             }
         }
-        __threadfence();
-        if (ld_volatile_i32(&ctl->abort)) ok = 0;
+        __threadfence();  // the other blocks' writes before this block's next reads
         s_ok = ok;
     }
     __syncthreads();

@@ -92,7 +92,7 @@ struct PeelArgs {
 
 __device__ __forceinline__ void set_status(PeelCtl* c, int s) {
     atomicMax(&c->g.status, s);
-    atomicExch(&c->g.abort, 1);
+    grid_abort(&c->g);
 }
 
 __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long* p) {
