@@ -544,7 +544,7 @@ def bench_served_small(dev, srv, num_graphs=4096, rate=20000.0):
 # `bench.py --steps 1 --warmup 1 --no-cpu-baseline --no-batched --no-served`
 # (summarised in profiles/launches_rmat_s22_bench.md).
 MEASURED_TRAFFIC = {
-    (22, 16): {"support": 32.97e9, "listing": 152.4e9, "peel": 281.62e9, "outputs": 6.6e9, "setup": 2.4e9},
+    (22, 16): {"support": 31.30e9, "listing": 150.5e9, "peel": 284.37e9, "outputs": 6.6e9, "setup": 2.4e9},
 }
 
 
