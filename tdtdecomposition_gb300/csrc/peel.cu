@@ -1289,7 +1289,17 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
                            ? (unsigned long long)g_fixed_cand_cap : kFixedCandCap;
     A.ctl = L.ctl;
     if (di.sms * occ > 4096) occ = 4096 / di.sms;
-    dim3 grid(di.sms * occ), block(kPeelBlock);
+    // Smaller graphs peel their lists faster on fewer blocks: the sub-rounds
+    // are short, so the grid barrier and the idle warps cost more than the
+    // parallelism gives (R-MAT scale 10-18 measured 4-15 % faster on one block
+    // per SM, scales 10-14 on one per two SMs; scale 20 and up fastest on
+    // all).  The search peel (no list tail) keeps every block: its slots are
+    // binary searches, and scale 18 ran 22 % slower on half the blocks.
+    int nblk = di.sms * occ;
+    if (tail > 0 && E < (1ll << 18)) nblk = (di.sms + 1) / 2;
+    else if (tail > 0 && E < (1ll << 22)) nblk = di.sms;
+    if (nblk > di.sms * occ) nblk = di.sms * occ;
+    dim3 grid(nblk), block(kPeelBlock);
     void* args[] = {&A};
     TDT_CUDA(cudaLaunchCooperativeKernel((void*)peel_kernel, grid, block, args, 0, st));
     note_launch();
