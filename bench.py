@@ -440,7 +440,7 @@ def bench_undirected(dev, scale=18):
 
 
 # ---------------------------------------------------------------- served workload
-def bench_served(dev, n_requests=48, rates=(8.0, 32.0, 128.0)):
+def bench_served(dev, n_requests=48, rates=(8.0, 32.0, 128.0, 512.0, 2048.0)):
     """Poisson request streams (the same 48 seeded requests replayed at each
     rate): half Barabasi-Albert (n log-uniform [256, 2^18], m in {4..16}),
     half R-MAT (scale 12..20, edge factor 16); half full decompositions, half
@@ -457,15 +457,18 @@ def bench_served(dev, n_requests=48, rates=(8.0, 32.0, 128.0)):
     gb, _ = preprocess_edges(big.src.to(dev), big.dst.to(dev), workspace=pps)
     T.truss_decompose(gb, workspace=wsp, list_budget=S.DEFAULT_LIST_BUDGET)
     del gb
-    plain_answers, edges = [], 0
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    for r in base:
-        g, _ = preprocess_edges(r.src.to(dev, non_blocking=True), r.dst.to(dev, non_blocking=True), workspace=pps)
-        edges += g.num_edges
-        res = T.truss_decompose(g, workspace=wsp, list_budget=S.DEFAULT_LIST_BUDGET)
-        plain_answers.append(S.answer_for(r.query, res.truss).cpu())
-    s_plain = time.perf_counter() - t1
+    s_plain = float("inf")
+    for _ in range(2):  # the faster of two passes (the plain time varies between passes)
+        plain_answers, edges = [], 0
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for r in base:
+            g, _ = preprocess_edges(r.src.to(dev, non_blocking=True), r.dst.to(dev, non_blocking=True),
+                                    workspace=pps)
+            edges += g.num_edges
+            res = T.truss_decompose(g, workspace=wsp, list_budget=S.DEFAULT_LIST_BUDGET)
+            plain_answers.append(S.answer_for(r.query, res.truss).cpu())
+        s_plain = min(s_plain, time.perf_counter() - t1)
     out = {"workload": "Poisson stream of %d requests: half BA n log-uniform [256,2^18] m {4..16}, half R-MAT "
                        "scale 12..20 ef 16; half decompose, half k-truss k in [3,20]; 150 GB budget" % n_requests,
            "requests": n_requests, "edges": edges, "draws": draws,

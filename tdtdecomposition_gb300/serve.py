@@ -74,13 +74,15 @@ DEFAULT_LIST_BUDGET = 24e9
 
 
 class TrussServer:
-    def __init__(self, device=None, memory_budget=150e9, max_batch_edges=1 << 28, list_budget=DEFAULT_LIST_BUDGET):
+    def __init__(self, device=None, memory_budget=150e9, max_batch_edges=1 << 28, list_budget=DEFAULT_LIST_BUDGET,
+                 max_group_draws=1 << 23):
         dev = torch.device(device) if device is not None else torch.device("cuda")
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
         self.device = dev
         self.budget = float(memory_budget)
         self.max_batch_edges = int(max_batch_edges)
+        self.max_group_draws = int(max_group_draws)
         self.list_budget = int(list_budget)  # workspace tail for triangle lists (device decides per batch)
         self.ingest_stream = torch.cuda.Stream(self.device)
         self.compute_stream = torch.cuda.Stream(self.device)
@@ -89,24 +91,30 @@ class TrussServer:
 
     # ------------------------------------------------------------ ingest
     def _ingest_loop(self, inbox, ready):
-        """Ingests every request admitted so far as one group: one host-to-
-        device copy of their concatenated edge lists and one grouped
-        preprocessing call (vertex ids shifted per request, ranks grouped per
-        request), so a group of small requests costs one set of launches."""
+        """Ingests the requests admitted so far as one group, up to
+        max_group_draws edge draws: one host-to-device copy of their
+        concatenated edge lists and one grouped preprocessing call (vertex ids
+        shifted per request, ranks grouped per request), so a group of small
+        requests costs one set of launches.  The cap lets the decomposition of
+        a first group start while a burst of arrivals is still being
+        ingested."""
         torch.cuda.set_device(self.device)
         with torch.cuda.stream(self.ingest_stream):
             stop = False
             while not stop:
                 group = [inbox.get()]
-                while True:
+                draws = len(group[0].src) if group[0] is not None else 0
+                while group[-1] is not None and draws < self.max_group_draws:
                     try:
-                        group.append(inbox.get_nowait())
+                        r = inbox.get_nowait()
                     except queue.Empty:
                         break
+                    group.append(r)
+                    if r is not None:
+                        draws += len(r.src)
                 if group[-1] is None:
                     stop = True
                     group = group[:-1]
-                group = [r for r in group if r is not None]
                 if not group:
                     continue
                 chunk = self._ingest_group(group)
