@@ -73,6 +73,24 @@ def answer_for(query, truss_slice):
 DEFAULT_LIST_BUDGET = 24e9
 
 
+def take_group(inbox, max_draws):
+    """The next ingest group: block for one request, then take what is
+    already queued while the group holds fewer than max_draws edge draws.
+    None in the queue ends the stream.  Returns (group, stop)."""
+    group = [inbox.get()]
+    draws = len(group[0].src) if group[0] is not None else 0
+    while group[-1] is not None and draws < max_draws:
+        try:
+            r = inbox.get_nowait()
+        except queue.Empty:
+            break
+        group.append(r)
+        if r is not None:
+            draws += len(r.src)
+    stop = group[-1] is None
+    return (group[:-1] if stop else group), stop
+
+
 class TrussServer:
     def __init__(self, device=None, memory_budget=150e9, max_batch_edges=1 << 28, list_budget=DEFAULT_LIST_BUDGET,
                  max_group_draws=1 << 23):
@@ -102,23 +120,9 @@ class TrussServer:
         with torch.cuda.stream(self.ingest_stream):
             stop = False
             while not stop:
-                group = [inbox.get()]
-                draws = len(group[0].src) if group[0] is not None else 0
-                while group[-1] is not None and draws < self.max_group_draws:
-                    try:
-                        r = inbox.get_nowait()
-                    except queue.Empty:
-                        break
-                    group.append(r)
-                    if r is not None:
-                        draws += len(r.src)
-                if group[-1] is None:
-                    stop = True
-                    group = group[:-1]
-                if not group:
-                    continue
-                chunk = self._ingest_group(group)
-                ready.put(chunk)
+                group, stop = take_group(inbox, self.max_group_draws)
+                if group:
+                    ready.put(self._ingest_group(group))
 
     def _ingest_group(self, group):
         nids = []

@@ -1,5 +1,5 @@
 """Host-side logic that needs no GPU: generators, argument checks of the
-drop-in operators, the CSRCOO container."""
+drop-in operators, the CSRCOO container, the server's ingest grouping."""
 import numpy as np
 import pytest
 import torch
@@ -72,3 +72,32 @@ def test_research_operators_check_their_arguments():
     assert all(not getattr(tt, n).__doc__ is None for n in tt.__all__)
     assert len([n for n in tt.__all__ if not n.endswith("_k") and "AffectedSupport" not in n
                 or n.startswith("sub_AllAffected")]) >= 20
+
+
+def test_server_ingest_groups_are_capped():
+    """The server's ingest takes what is queued up to a draw cap, so a burst
+    is split into groups and the first decomposition starts early."""
+    import queue
+    from tdtdecomposition_gb300 import serve as S
+
+    def req(i, n):
+        return S.Request(i, 0.0, torch.zeros(n, dtype=torch.int32), torch.zeros(n, dtype=torch.int32), "decompose")
+
+    q = queue.Queue()
+    for i in range(4):
+        q.put(req(i, 3))
+    q.put(None)
+    g, stop = S.take_group(q, 8)          # 3 + 3 < 8, the third reaches 9
+    assert [r.id for r in g] == [0, 1, 2] and not stop
+    g, stop = S.take_group(q, 8)          # the last request, then the end of the stream
+    assert [r.id for r in g] == [3] and stop
+
+    q.put(req(7, 20))
+    q.put(req(8, 1))
+    g, stop = S.take_group(q, 8)          # one request above the cap goes alone
+    assert [r.id for r in g] == [7] and not stop
+    g, stop = S.take_group(q, 8)          # nothing else queued: no wait for more
+    assert [r.id for r in g] == [8] and not stop
+
+    q.put(None)
+    assert S.take_group(q, 8) == ([], True)
