@@ -14,7 +14,8 @@ from tdtdecomposition_gb300 import formats as F
 from tdtdecomposition_gb300.graph import CSRCOO
 from tests import _golden as GD
 
-REF = "/root/reference"
+# the reference tree, where present: its loader and its binary-CSR tool pin the formats
+REF = os.environ.get("TDT_REFERENCE_ROOT", "/root/reference")
 
 
 def _write_text(path, pairs, header=True):
