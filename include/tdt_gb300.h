@@ -61,6 +61,15 @@ unsigned long long tdt_launch_count(void);
 int tdt_profile_start(int max_calls);
 int tdt_profile_stop(float *ms_phase, int *ncalls);
 
+/* Block 0's clock of the last decomposition or k-truss search run in
+ * `workspace` (diagnostic): ns[0] candidate processing, ns[1] grid-barrier
+ * waits after processing, ns[2] level changes, ns[3] the whole persistent
+ * peel kernel.  Synchronises `stream`.  The phases also appear as NVTX
+ * ranges ("tdt support", "tdt listing", "tdt peel", "tdt outputs") when a
+ * profiler is attached.  The reference times its phases with host clocks
+ * around synchronize calls (demo_truss/singlegpu_truss.py:69-77, :153-157). */
+int tdt_peel_clock(const void *workspace, long long *ns, cudaStream_t stream);
+
 /* Testing knob of the support/listing kernels: rows with out-degree <=
  * warp_cap are processed by one warp, heavier rows by a block with the row
  * staged in shared memory up to heavy_cap entries, and beyond that in place.

@@ -64,7 +64,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

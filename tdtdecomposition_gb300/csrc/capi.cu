@@ -3,6 +3,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 
 namespace tdt {
@@ -20,9 +22,28 @@ struct PhaseRec {
 static PhaseRec* g_prof = nullptr;
 static int g_prof_cap = 0, g_prof_n = 0, g_prof_on = 0;
 
+// NVTX ranges of the phases on the calling thread (no-ops unless a profiler
+// is attached).  A call that ended early between two marks leaves its range
+// open; the next call's start closes it.
+static thread_local int t_nvtx_depth = 0;
+static const char* const kPhaseNames[4] = {"tdt support", "tdt listing", "tdt peel", "tdt outputs"};
+static void nvtx_mark(int phase) {
+    if (phase == 0) {
+        for (; t_nvtx_depth > 0; t_nvtx_depth--) nvtxRangePop();
+    } else if (t_nvtx_depth > 0) {
+        nvtxRangePop();
+        t_nvtx_depth--;
+    }
+    if (phase >= 0 && phase < 4) {
+        nvtxRangePushA(kPhaseNames[phase]);
+        t_nvtx_depth++;
+    }
+}
+
 // Called by run_peel: phase 0 = start, 1 = after the support pass, 2 = after
 // the listing pass, 3 = after the peel, 4 = end.
 void prof_mark(int phase, cudaStream_t st) {
+    nvtx_mark(phase);
     if (!g_prof_on) return;
     if (phase == 0) {
         if (g_prof_n >= g_prof_cap) return;
@@ -91,6 +112,7 @@ void set_support_caps(int warp_cap, int heavy_cap);
 void set_peel_deadline(long long ns);
 void set_fixed_caps(long long items, long long cands);
 void set_peel_dyn_min(long long slots);
+int peel_clock(const void* ws, long long* ns, cudaStream_t st);
 int test_barrier_timeout(void* ws, long long limit_ns, cudaStream_t st);
 int launch_support_accum_i32(const int32_t* rp, int32_t stride, const int32_t* cols, int64_t nv, int64_t ne,
                              int32_t* out, cudaStream_t st);
@@ -134,6 +156,9 @@ API void tdt_set_support_caps(int warp_cap, int heavy_cap) { set_support_caps(wa
 API void tdt_set_peel_deadline_ns(long long ns) { set_peel_deadline(ns); }
 API void tdt_set_ktruss_batch_caps(long long items, long long cands) { set_fixed_caps(items, cands); }
 API void tdt_set_peel_dynamic_min(long long slots) { set_peel_dyn_min(slots); }
+API int tdt_peel_clock(const void* workspace, long long* ns, cudaStream_t stream) {
+    return peel_clock(workspace, ns, stream);
+}
 API int tdt_test_barrier_timeout(void* workspace, long long limit_ns, cudaStream_t stream) {
     return test_barrier_timeout(workspace, limit_ns, stream);
 }

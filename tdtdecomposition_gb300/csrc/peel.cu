@@ -1069,6 +1069,19 @@ void set_peel_deadline(long long ns) { g_peel_deadline_ns = ns; }
 
 // Test hook: lower the k-truss collection batch limits (<= 0: the defaults).
 static long long g_dyn_min_slots = 0;
+
+// Block 0's clock of the last persistent peel run in this workspace (the
+// control block sits at its start): processing, grid-barrier waits after
+// processing, level changes, and the whole kernel, in ns.
+int peel_clock(const void* ws, long long* ns, cudaStream_t st) {
+    TDT_CHECK_ARG(ws != nullptr && ns != nullptr, "null pointer");
+    const PeelCtl* ctl = reinterpret_cast<const PeelCtl*>(ws);
+    unsigned long long t[4];
+    TDT_CUDA(cudaMemcpyAsync(t, &ctl->t_proc, sizeof(t), cudaMemcpyDeviceToHost, st));
+    TDT_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < 4; i++) ns[i] = (long long)t[i];
+    return TDT_OK;
+}
 void set_peel_dyn_min(long long slots) { g_dyn_min_slots = slots; }
 static long long g_fixed_item_cap = 0, g_fixed_cand_cap = 0;
 void set_fixed_caps(long long items, long long cands) {

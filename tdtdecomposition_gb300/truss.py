@@ -7,6 +7,7 @@ with untiled row offsets; results are keyed by CSR edge position, like the
 reference's e_truss (singlegpu_truss.py:83-101 keeps original positions in
 ``edges``).
 """
+import ctypes
 from typing import NamedTuple
 
 import torch
@@ -200,3 +201,45 @@ def triangle_count(graph, workspace=None, stream=None, return_support=False):
     _check_stats(sh, "tdt_triangle_count")
     T = int(sh[STAT_TRIANGLES])
     return (T, support) if return_support else T
+
+
+PHASES = ("support", "listing", "peel", "outputs")
+
+
+class PhaseProfile:
+    """Phase times of the whole-path calls made inside a ``with`` block,
+    from CUDA events recorded on their streams (tdt_profile_start /
+    tdt_profile_stop): ``ms[phase]`` summed over the calls, ``calls`` the
+    number recorded.  The reference prints host-clock times of its support
+    and peel phases (singlegpu_truss.py:69-77, :153-157)."""
+
+    def __init__(self, max_calls=4096):
+        self.max_calls = int(max_calls)
+        self.ms = None
+        self.calls = 0
+
+    def __enter__(self):
+        _lib.check(_lib.load().tdt_profile_start(self.max_calls), "tdt_profile_start")
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        ph = (ctypes.c_float * 4)()
+        n = ctypes.c_int()
+        rc = _lib.load().tdt_profile_stop(ph, ctypes.byref(n))
+        if exc_type is None:
+            _lib.check(rc, "tdt_profile_stop")
+        self.ms = dict(zip(PHASES, (float(x) for x in ph)))
+        self.calls = n.value
+        return False
+
+
+def peel_clock(workspace, stream=None):
+    """Block 0's clock (ms) of the last peel run in `workspace`: candidate
+    processing, grid-barrier waits, level changes and the whole kernel."""
+    if workspace is None or workspace.buf is None:
+        raise ValueError("peel_clock needs the Workspace the decomposition ran in")
+    ns = (ctypes.c_longlong * 4)()
+    s = (stream or torch.cuda.current_stream(workspace.buf.device)).cuda_stream
+    with torch.cuda.device(workspace.buf.device):
+        _lib.check(_lib.load().tdt_peel_clock(workspace.buf.data_ptr(), ns, s), "tdt_peel_clock")
+    return dict(zip(("processing", "barrier_waits", "level_changes", "total"), (x / 1e6 for x in ns)))

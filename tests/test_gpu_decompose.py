@@ -290,3 +290,21 @@ def test_search_peel_dynamic_ranges(scale):
     for r in (static, dyn):
         assert r.kmax == ref.kmax and torch.equal(r.truss, ref.truss) and torch.equal(r.e_truss, ref.e_truss)
     assert torch.equal(kt, ref.truss >= max(3, ref.kmax // 2))
+
+
+def test_phase_profile_and_peel_clock():
+    """Phase times (CUDA events on the call's stream) of two decompositions,
+    and block 0's clock of the last peel."""
+    s, d = G.rmat_edges(12, 16 << 12, seed=1)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
+    g = graph_of(rows, cols, rp)
+    ws = T.Workspace()
+    T.truss_decompose(g, workspace=ws)
+    with T.PhaseProfile() as prof:
+        for _ in range(2):
+            res = T.truss_decompose(g, workspace=ws)
+    assert res.listed and prof.calls == 2
+    assert all(prof.ms[p] > 0 for p in T.PHASES)
+    clk = T.peel_clock(ws)
+    assert 0 < clk["processing"] <= clk["total"]
+    assert clk["barrier_waits"] >= 0 and clk["level_changes"] >= 0
