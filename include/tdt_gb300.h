@@ -57,7 +57,8 @@ unsigned long long tdt_launch_count(void);
  * them and writes the summed milliseconds of four phases to ms_phase[4]
  * (host): [0] the support pass, [1] the triangle-listing pass, [2] the peel
  * (in-adjacency build and the persistent peel kernel), [3] the outputs; and
- * the number of calls recorded to *ncalls. */
+ * the number of calls recorded to *ncalls.  The recording is process-wide:
+ * start and stop it while no other thread makes whole-path calls. */
 int tdt_profile_start(int max_calls);
 int tdt_profile_stop(float *ms_phase, int *ncalls);
 

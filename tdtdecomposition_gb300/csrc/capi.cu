@@ -3,6 +3,9 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
+#include <mutex>
+
 #include <nvtx3/nvToolsExt.h>
 
 #include "common.cuh"
@@ -65,12 +68,16 @@ int cuda_status(cudaError_t e, const char* what) {
     return e == cudaErrorMemoryAllocation ? TDT_ERR_WORKSPACE : TDT_ERR_CUDA;
 }
 
+// Per-device attributes, cached.  Calls come from several host threads (the
+// server ingests on one and decomposes on another): a cache entry is
+// published with a release store of its flag after it is written, and read
+// only after an acquire load of the flag sees it.
 int device_info(DeviceInfo* out) {
     static DeviceInfo cache[64];
-    static bool have[64] = {false};
+    static std::atomic<bool> have[64];
     int dev = 0;
     TDT_CUDA(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && have[dev]) {
+    if (dev >= 0 && dev < 64 && have[dev].load(std::memory_order_acquire)) {
         *out = cache[dev];
         return TDT_OK;
     }
@@ -85,9 +92,13 @@ int device_info(DeviceInfo* out) {
                   di.cc_minor);
         return TDT_ERR_UNSUPPORTED;
     }
-    if (dev >= 0 && dev < 64) {
-        cache[dev] = di;
-        have[dev] = true;
+    if (dev >= 0 && dev < 64 && !have[dev].load(std::memory_order_acquire)) {
+        static std::mutex m;
+        std::lock_guard<std::mutex> lk(m);
+        if (!have[dev].load(std::memory_order_relaxed)) {
+            cache[dev] = di;
+            have[dev].store(true, std::memory_order_release);
+        }
     }
     *out = di;
     return TDT_OK;
