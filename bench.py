@@ -602,6 +602,7 @@ def main_ours(args):
     phases = (ctypes.c_float * 4)()
     nc = ctypes.c_int()
     L.tdt_profile_stop(phases, ctypes.byref(nc))
+    peel_clk = T.peel_clock(wsp)  # block 0's split of the last timed peel
     clk = clocks.stop() if clocks else None
     t_ms = ev0.elapsed_time(ev1)
     t_ms = max_over_ranks(t_ms, ws, dev)
@@ -681,6 +682,7 @@ def main_ours(args):
     roof = {"bound": "hbm", "kernel": "decomposition (all kernels of one step)", "achieved": ach, "peak": peak,
             "unit": "GB/s", "frac": ach / peak, "traffic": sum(mt.values()) if mt else None,
             "algorithmic_bytes": B_dec, "peak_source": peak_src, "per_kernel": per_kernel, "phase_ms": phases_ms,
+            "peel_clock_ms": {k: round(v, 2) for k, v in peel_clk.items()},
             "traffic_source": "ncu capture of this workload (profiles/launches_rmat_s22_bench.md)" if mt else None}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
