@@ -691,7 +691,9 @@ def main_ours(args):
                        "scale": scale, "edge_factor": ef, "abcd": [0.57, 0.19, 0.19, 0.05], "seed": 1,
                        "V": V, "E": E, "W": W, "kmax": res.kmax, "triangles": res.triangles,
                        "rounds": res.rounds, "parallelism": "replicas" if ws > 1 else "single",
-                       "triangle_lists": "kept (listed peel)" if res.listed else "none (search peel)",
+                       "triangle_lists": {2: "one walk counts and lists (listed peel)",
+                                          1: "count walk + listing walk (listed peel)"}.get(
+                                              res.listing, "none (search peel)"),
                        "l2": "inputs larger than L2 (CSR %.0f MB + in-adjacency)" % ((8 * E + 8 * V) / 1e6)},
             "roofline": roof,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -78,6 +78,13 @@ int tdt_peel_clock(const void *workspace, long long *ns, cudaStream_t stream);
  * defaults.  Affects calls launched afterwards from any thread. */
 void tdt_set_support_caps(int warp_cap, int heavy_cap);
 
+/* Testing knob of the support/listing kernels: 0 makes their wedge walk load
+ * one column index per lane and step, 1 (the default) four at a time from
+ * 16-byte chunks (used when the columns array is 16-byte aligned and the
+ * graph has fewer than 2^30 edges).  Results do not depend on it.  Affects
+ * calls launched afterwards from any thread. */
+void tdt_set_vector_walk(int on);
+
 /* Testing knobs of the failure paths (no counterpart in the reference, which
  * has no bounded waits).  tdt_set_peel_deadline_ns: wall-clock budget of the
  * peel launches that follow (<= 0 restores the default of 120 s); a run past
@@ -338,15 +345,22 @@ enum tdt_stat_index {
     TDT_STAT_TRIANGLES = 4,  /* triangle count                                 */
     TDT_STAT_NETRUSS = 5,    /* entries written to e_truss                     */
     TDT_STAT_ALIVE = 6,      /* k-truss search: edges left in the k-truss      */
-    TDT_STAT_LISTED = 7,     /* 1: the peel read per-edge triangle lists; 0: it searched */
+    TDT_STAT_LISTED = 7,     /* how the peel found each peeled edge's triangles: 0 by search in
+                                the adjacency; per-edge triangle lists, 1 written by a second walk,
+                                2 packed from the one walk that also counted them */
     TDT_STAT_COUNT = 8
 };
 
 /* Workspace for tdt_truss_decompose / tdt_ktruss_search / tdt_triangle_count.
- * Workspace bytes beyond this size (rounded up to 256) hold per-edge triangle
- * lists: when 24 * T bytes fit there (T = triangle count), the peel reads each
- * peeled edge's triangles from its list; otherwise it finds them by binary
- * search in the adjacency.  Results are identical either way. */
+ * Workspace bytes beyond this size (rounded up to 256), the list tail, hold
+ * per-edge triangle lists: when 24 * T bytes fit there (T = triangle count),
+ * the peel reads each peeled edge's triangles from its list; otherwise it
+ * finds them by binary search in the adjacency.  When the tail also holds the
+ * staging area of the one walk (8 bytes per slot of the per-edge bounds
+ * min(d+(u)-i-1, d+(v)) + min(i, d-(v)-1), edge (u,v) at position i of row
+ * u), one walk counts the triangles and writes the lists; otherwise a
+ * count-only walk runs first and a second walk writes them.  Results are
+ * identical every way. */
 size_t tdt_decompose_workspace_bytes(int64_t num_vertices, int64_t num_edges);
 
 /* Full truss decomposition: the single-call replacement of the `--cuda` flow
@@ -379,15 +393,16 @@ int tdt_triangle_count(const int32_t *cols, const int64_t *row_ptr, int64_t num_
  * need the count (another component owns the device allocator, or the path
  * must not stall on an allocation).  Same outputs as tdt_triangle_count
  * (support may be NULL; stats[TDT_STAT_TRIANGLES], stats[TDT_STAT_STATUS]),
- * but the scratch is a fixed 24 MiB array inside the library, held on every
+ * but the scratch is a fixed 40 MiB array inside the library, held on every
  * GPU that loads it until the process exits.  Limit: at most 2^18 vertices
  * and 2^18 edges; larger graphs return TDT_ERR_INVALID (use
  * tdt_triangle_count).  The first call on a device looks up that array's
  * address (cudaGetSymbolAddress) with the device current; make that first
- * call before any stream capture.  All calls share the array and each call
- * re-initialises what it uses, so two calls that overlap on the same GPU
- * (for example on two streams) race on it and must be serialised by the
- * caller. */
+ * call before any stream capture, and do not call it across a
+ * cudaDeviceReset (the cached address would be stale).  All calls share the
+ * array and each call re-initialises what it uses, so two calls that overlap
+ * on the same GPU (for example on two streams) race on it and must be
+ * serialised by the caller. */
 int tdt_triangle_count_noalloc(const int32_t *cols, const int64_t *row_ptr, int64_t num_vertices,
                                int64_t num_edges, int32_t *support, int64_t *stats, tdt_stream_t stream);
 

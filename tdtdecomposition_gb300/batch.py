@@ -113,7 +113,7 @@ class CapturedBatch:
         self.stats = torch.zeros(T.STAT_COUNT, dtype=torch.int64, device=dev)
         wso = T._ws_for(dev, workspace)
         base = (L.tdt_decompose_workspace_bytes(V, E) + 255) // 256 * 256
-        tail = int(list_budget) if list_budget is not None else T._list_bytes(wso, cols, rp, lists, base)
+        tail = int(list_budget) if list_budget is not None else T._list_bytes(wso, cols, rp, lists, base, rows)
         self.ws = wso.get(base + tail)
         self.ws_bytes = base + tail
         eo = batch.edge_offsets.to(dev)

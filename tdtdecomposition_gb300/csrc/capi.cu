@@ -120,6 +120,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
              uint8_t* in_k, int32_t* support_out, int64_t* stats, void* ws, size_t ws_bytes, cudaStream_t st);
 
 void set_support_caps(int warp_cap, int heavy_cap);
+void set_vector_walk(int on);
 void set_peel_deadline(long long ns);
 void set_fixed_caps(long long items, long long cands);
 void set_peel_dyn_min(long long slots);
@@ -164,6 +165,7 @@ API const char* tdt_last_error(void) { return g_err; }
 API unsigned long long tdt_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
 API void tdt_set_support_caps(int warp_cap, int heavy_cap) { set_support_caps(warp_cap, heavy_cap); }
+API void tdt_set_vector_walk(int on) { set_vector_walk(on); }
 API void tdt_set_peel_deadline_ns(long long ns) { set_peel_deadline(ns); }
 API void tdt_set_ktruss_batch_caps(long long items, long long cands) { set_fixed_caps(items, cands); }
 API void tdt_set_peel_dynamic_min(long long slots) { set_peel_dyn_min(slots); }

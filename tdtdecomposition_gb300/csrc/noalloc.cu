@@ -27,13 +27,17 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
 
 constexpr int64_t kNoAllocMaxVertices = 1 << 18;
 constexpr int64_t kNoAllocMaxEdges = 1 << 18;
-constexpr size_t kNoAllocScratchBytes = 24ull << 20;  // 24 MiB: the workspace of 2^18 vertices and edges
+// 40 MiB: holds the workspace of kNoAllocMaxVertices vertices and
+// kNoAllocMaxEdges edges (35.2 MiB); the first call checks that it does.
+constexpr size_t kNoAllocScratchBytes = 40ull << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Host code cannot use g_noalloc_scratch as an address (on the host the name
 // only stands for the symbol), so each device's address is looked up once,
-// with that device current, and cached.
+// with that device current, and cached.  A cudaDeviceReset by the caller
+// unloads the module and makes the cached address stale: this entry point
+// must not be used across a cudaDeviceReset.
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_addr[64] = {nullptr};
 
@@ -46,6 +50,12 @@ static int noalloc_scratch(void** out) {
     }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (!g_noalloc_addr[dev]) {
+        const size_t at_limit = decompose_workspace_bytes(kNoAllocMaxVertices, kNoAllocMaxEdges);
+        if (at_limit > kNoAllocScratchBytes) {
+            set_error("tdt_triangle_count_noalloc: the workspace of its size limit (%zu bytes) exceeds the static "
+                      "scratch (%zu bytes)", at_limit, kNoAllocScratchBytes);
+            return TDT_ERR_UNSUPPORTED;
+        }
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");

@@ -46,8 +46,10 @@ constexpr uint64_t kPeelDeadlineNs = 120ull * 1000ull * 1000ull * 1000ull;
 
 struct PeelCtl {
     GridCtl g;
-    unsigned long long q[3];      // packed (items << kCandBits | candidates) per round slot
-    unsigned long long fe[3];     // frontier edges per round slot (queued or not)
+    // round r's counters live at r & 3: round r reads slot r, appends to r+1,
+    // sets the dead bits of round r-1's edges, and the top of round r clears r+2
+    unsigned long long q[4];      // packed (items << kCandBits | candidates) per round slot
+    unsigned long long fe[4];     // frontier edges per round slot (queued or not)
     unsigned long long cnt[3];     // survivors written by level change t, at t % 3
     unsigned long long side_n[3];  // side-list length of level-change pass k, at k % 3
     unsigned long long pfe[3];     // edges queued by level-change pass k, at k % 3
@@ -55,16 +57,19 @@ struct PeelCtl {
     int dmin[2];                   // minimum decrement result above the level during level L_t, at t & 1
     long long passes;              // level-change passes run (diagnostic)
     int listed;                   // 1: per-edge triangle lists were built (they fit the workspace)
-    int list_skip;                // gate of the listing pass and of the list-only setup kernels
-    int enum_skip;                // unused (the in-adjacency is always built)
-    int pad0;
+    int list_skip;                // gate of the role-C transpose (no lists)
+    int rewalk_skip;              // gate of the second walk (lists written by kSupList)
+    int compact_skip;             // gate of the staging compaction (lists from the one-walk pass)
+    int stage_skip;               // gate of the one-walk pass (kSupStage)
+    int roles_skip;               // gate of the count-only walk (kSupRoles)
+    int pad0[2];
     long long rounds;
     long long triangles;
     unsigned long long alive;
     // block 0's time (ns) in candidate processing, grid-barrier waits after
     // processing, and level transitions; diagnostic only
     unsigned long long t_proc, t_wait, t_trans, t_total;
-    unsigned long long grab[3];    // slot cursor of search-mode sub-round r, at r % 3
+    unsigned long long grab[4];    // slot cursor of search-mode sub-round r, at r & 3
 };
 
 struct PeelArgs {
@@ -76,9 +81,15 @@ struct PeelArgs {
     const int32_t* in_eid;
     int2* es;             // edge state {support, round}: round -1 = alive, else the sub-round that peeled it
     int32_t* round_level;
-    int4* qi[2];
-    long long* qb[2];
+    // queue of round r in buffer r % 3: round r reads r, appends r+1, and the
+    // items of round r-1 stay intact for the dead bits set during round r
+    int4* qi[3];
+    long long* qb[3];
     int32_t* alive[2];    // compacted alive-edge lists (level transitions)
+    // bit e set: edge e was peeled in a sub-round before the current one (a
+    // filter in L2 that keeps most dead triangles away from the edge states;
+    // a bit not set yet only costs the state check it would have saved)
+    unsigned* dead;
     const int64_t* off;   // listed mode: list offsets int64[E+1]
     const int2* lists;    // listed mode: partner edge pairs
     int64_t V, E, round_cap;
@@ -376,8 +387,10 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
         g = a < b ? a : b;
     }
     const int32_t gw_end = g > INT32_MAX - kSideWindow ? INT32_MAX : g + kSideWindow;
-    const int slot = r_next % 3, buf = r_next & 1;
-    int2* side = reinterpret_cast<int2*>(A.qi[buf ^ 1]);  // the finished round's queue is free
+    const int slot = r_next & 3, buf = r_next % 3;
+    // buffer r_next + 1 = r_next - 2 is free: the dead bits of its items were
+    // set during round r_next - 1 (the finished round's items are still needed)
+    int2* side = reinterpret_cast<int2*>(A.qi[(r_next + 1) % 3]);
     AppendBuf B{app_e + (threadIdx.x / kWarp) * kAppBuf, 0, 0ull};
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         A.ctl->cnt[(t + 1) % 3] = 0;
@@ -575,7 +588,7 @@ __device__ __forceinline__ void warp_append_capped(const PeelArgs& A, bool liste
 __device__ bool fixed_collect(const PeelArgs& A, bool listed, int32_t l, int r_next, int& np) {
     const unsigned lane = lane_id();
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-    const int slot = r_next % 3, buf = r_next & 1;
+    const int slot = r_next & 3, buf = r_next % 3;
     pass_start(A, np);
     for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; base < A.E;
          base += nthreads) {
@@ -649,6 +662,7 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
         f = __ldg(A.in_eid + kk);
     }
     if (w == y) return false;
+    if ((A.dead[f >> 5] >> (f & 31)) & 1u) return false;  // (x,w) peeled before this round
     const int64_t gg = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
                                : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
     g = (int32_t)gg;
@@ -668,8 +682,8 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     const unsigned lane = lane_id();
     const unsigned le = lanemask_lt() | (1u << lane);
     int32_t dm = INT32_MAX;
-    const int slot = r % 3, buf = r & 1;
-    const int nslot = (r + 1) % 3, nbuf = buf ^ 1;
+    const int slot = r & 3, buf = r % 3;
+    const int nslot = (r + 1) & 3, nbuf = (r + 1) % 3;
     const int wib = threadIdx.x / kWarp;
     AppendBuf B{app_e + wib * kAppBuf, 0, 0ull};
     const unsigned long long packed = ld_cg_u64(&A.ctl->q[slot]);
@@ -677,6 +691,17 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     const long long T = (long long)(packed & kCandMask);
     const long long* __restrict__ qb = A.qb[buf];
     const int4* __restrict__ qi = A.qi[buf];
+    // the edges of round r-1 are dead from this round on: set their bits (a
+    // bit read before it is set only sends that triangle to the state check)
+    if (r > 0) {
+        long long nprev = (long long)(ld_cg_u64(&A.ctl->q[(r - 1) & 3]) >> kCandBits);
+        if (nprev > A.E) nprev = A.E;
+        const int4* __restrict__ qp = A.qi[(r - 1) % 3];
+        for (long long i = gwarp * kWarp + lane; i < nprev; i += nwarps * kWarp) {
+            const int32_t e = __ldcg(&qp[i].x);
+            atomicOr(A.dead + (e >> 5), 1u << (e & 31));
+        }
+    }
     // listed mode: each warp owns a contiguous range of candidate slots (a
     // multiple of 64).  Search mode with many slots: warps take ranges of
     // kDynChunk slots from a shared cursor (the binary search of a slot costs
@@ -726,6 +751,20 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         bool tra = false, trb = false;
         if (va) tra = slot_edges<Listed>(A, ita, ta - wa.base_l, fa, ga);
         if (vb) trb = slot_edges<Listed>(A, itb, tb - wb.base_l, fb, gb);
+        // dead-bit filter: a triangle with an edge peeled before round r is gone
+        {
+            unsigned xa = 0, ya = 0, xb = 0, yb = 0;
+            if (tra) {
+                xa = A.dead[fa >> 5];
+                ya = A.dead[ga >> 5];
+            }
+            if (trb) {
+                xb = A.dead[fb >> 5];
+                yb = A.dead[gb >> 5];
+            }
+            if (tra && (((xa >> (fa & 31)) | (ya >> (ga & 31))) & 1u)) tra = false;
+            if (trb && (((xb >> (fb & 31)) | (yb >> (gb & 31))) & 1u)) trb = false;
+        }
         int32_t rfa = -2, rga = -2, rfb = -2, rgb = -2;
         if (tra) {
             rfa = __ldcg(&A.es[fa].y);
@@ -818,9 +857,9 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const _
     for (;;) {
         if (master) {
             A.round_level[r] = l;
-            A.ctl->q[(r + 2) % 3] = 0;
-            A.ctl->fe[(r + 2) % 3] = 0;
-            A.ctl->grab[(r + 2) % 3] = 0;
+            A.ctl->q[(r + 2) & 3] = 0;
+            A.ctl->fe[(r + 2) & 3] = 0;
+            A.ctl->grab[(r + 2) & 3] = 0;
             if (globaltimer_ns() - t_start > A.deadline_ns) set_status(A.ctl, TDT_ERR_TIMEOUT);
         }
         // level L_t (t = ntrans - 1) folds its decrement results into dmin[t & 1]
@@ -838,9 +877,9 @@ __global__ void __launch_bounds__(kPeelBlock, TDT_PEEL_MINB) peel_kernel(const _
             if (master) set_status(A.ctl, TDT_ERR_CAPACITY);
             return;
         }
-        // fe[(r+1) % 3] is only written by sub-round r (level changes count
-        // into pfe), and cleared again at the top of sub-round r+2
-        if (ld_cg_u64(&A.ctl->fe[(r + 1) % 3]) == 0) {
+        // fe[(r+1) & 3] is only written by sub-round r (level changes count
+        // into pfe), and cleared again at the top of sub-round r+3
+        if (ld_cg_u64(&A.ctl->fe[(r + 1) & 3]) == 0) {
             if (A.mode != 0) {
                 // k-truss search: the next batch of low-support edges, if any
                 if (!fixed_collect(A, listed, l, r + 1, np)) break;
@@ -948,22 +987,111 @@ __global__ void init_state_kernel(const int32_t* __restrict__ cA, const int32_t*
     }
 }
 
-// Lists fit when 8 bytes x (3T = off[E]) fit the workspace tail.
-__global__ void list_decide_kernel(const int64_t* __restrict__ off, int64_t E, unsigned long long tail_bytes,
-                                   int want_lists, PeelCtl* ctl) {
-    const unsigned long long need = 8ull * (unsigned long long)off[E];
-    const int ok = want_lists && ctl->g.status == 0 && need <= tail_bytes;
-    ctl->listed = ok;
-    ctl->list_skip = !ok;
-    ctl->enum_skip = ok;
+// Staging bounds of the one-walk pass, per edge e = (u, v) at position i of
+// row u: role A (triangles (u, v, w)) at most min(d+(u) - i - 1, d+(v)) --
+// w lies in N+(u) after v and in N+(v); role B (triangles (u, x, v), x in
+// N+(u) before v and in N-(v) \ {u}) at most min(i, d-(v) - 1).  bnd[e] =
+// the role-A bound, sz[e] = both (the staging region of e).
+__global__ void stage_bounds_kernel(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols,
+                                    const int64_t* __restrict__ rp, const int64_t* __restrict__ cp, int64_t E,
+                                    int32_t* __restrict__ bnd, int32_t* __restrict__ sz, const PeelCtl* ctl) {
+    if (*(volatile const int*)&ctl->g.status != 0) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = rows[e], v = cols[e];
+        const int64_t bu = rp[u];
+        const int64_t i = e - bu, du = rp[u + 1] - bu;
+        const int64_t dv = rp[v + 1] - rp[v], inv = cp[v + 1] - cp[v];
+        const int64_t a = du - i - 1 < dv ? du - i - 1 : dv;
+        const int64_t b = i < inv - 1 ? i : inv - 1;
+        const int64_t aa = a < 0 ? 0 : a, bb = b < 0 ? 0 : b;
+        bnd[e] = (int32_t)aa;
+        sz[e] = (int32_t)(aa + bb);  // < 2^31: the one-walk pass is only chosen for V < 2^30
+    }
 }
 
-// Global slot cursors of the listing pass (used by rows listed in place):
+// Count-only walk or one walk with staging: the one walk when the staging
+// regions (8 bytes x soff[E]) fit the list tail.
+__global__ void stage_decide_kernel(const int64_t* __restrict__ soff, int64_t E, int64_t V,
+                                    unsigned long long tail_bytes, int want_lists, PeelCtl* ctl) {
+    const int ok0 = ctl->g.status == 0;
+    const int st = ok0 && want_lists && V < (1ll << 30) && 8ull * (unsigned long long)soff[E] <= tail_bytes;
+    ctl->stage_skip = !st;
+    ctl->roles_skip = !ok0 || st;
+}
+
+// Global cursors of the one walk's staging slots (used by rows searched in
+// place): role A at soff[e], role B at soff[e] + bnd[e].
+__global__ void stage_cursor_kernel(const int64_t* __restrict__ soff, const int32_t* __restrict__ bnd, int64_t E,
+                                    unsigned long long* __restrict__ curA, unsigned long long* __restrict__ curB,
+                                    const PeelCtl* ctl) {
+    if (*(volatile const int*)&ctl->stage_skip) return;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long o = (unsigned long long)soff[e];
+        curA[e] = o;
+        curB[e] = o + (unsigned long long)bnd[e];
+    }
+}
+
+// Lists fit when 8 bytes x (3T = off[E]) fit the workspace tail.  After the
+// one walk they are packed from the staging area (which sits at the end of
+// the tail) when both fit side by side; otherwise, when the lists alone fit,
+// the second walk writes them; otherwise the peel searches.
+__global__ void list_decide_kernel(const int64_t* __restrict__ off, const int64_t* __restrict__ soff, int64_t E,
+                                   unsigned long long tail_bytes, int want_lists, PeelCtl* ctl) {
+    const unsigned long long need = 8ull * (unsigned long long)off[E];
+    const int ok0 = want_lists && ctl->g.status == 0;
+    const int staged = !ctl->stage_skip;
+    const unsigned long long stage = staged ? 8ull * (unsigned long long)soff[E] : 0ull;
+    const int compact = ok0 && staged && need <= tail_bytes - stage;
+    const int rewalk = ok0 && !compact && need <= tail_bytes;
+    ctl->listed = compact || rewalk;
+    ctl->list_skip = !(compact || rewalk);
+    ctl->compact_skip = !compact;
+    ctl->rewalk_skip = !rewalk;
+}
+
+// Pack the role-A / role-B entries of every edge from its staging region
+// (slot s at stage_end[-1-s]) into its final list: role A at off[e], role B
+// at off[e] + cA[e].  A warp takes 32 edges at a time (their offsets and
+// counts in one coalesced load each) and copies them one after the other.
+__global__ void stage_compact_kernel(const int64_t* __restrict__ soff, const int32_t* __restrict__ bnd,
+                                     const int32_t* __restrict__ cA, const int32_t* __restrict__ cB,
+                                     const int64_t* __restrict__ off, const int2* __restrict__ stage_end,
+                                     int2* __restrict__ lists, int64_t E, const PeelCtl* ctl) {
+    if (*(volatile const int*)&ctl->compact_skip) return;
+    const unsigned lane = lane_id();
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kWarp; base < E;
+         base += nw * kWarp) {
+        const int64_t e = base + lane;
+        int64_t so = 0, o = 0;
+        int32_t b = 0, na = 0, nb = 0;
+        if (e < E) {
+            so = soff[e];
+            b = bnd[e];
+            na = cA[e];
+            nb = cB[e];
+            o = off[e];
+        }
+        const int kn = E - base < kWarp ? (int)(E - base) : kWarp;
+        for (int k = 0; k < kn; k++) {
+            const int64_t sk = __shfl_sync(kFull, so, k), ok = __shfl_sync(kFull, o, k);
+            const int32_t bk = __shfl_sync(kFull, b, k), ak = __shfl_sync(kFull, na, k),
+                          ck = __shfl_sync(kFull, nb, k);
+            for (int j = (int)lane; j < ak; j += kWarp) lists[ok + j] = __ldcs(stage_end - 1 - (sk + j));
+            for (int j = (int)lane; j < ck; j += kWarp) lists[ok + ak + j] = __ldcs(stage_end - 1 - (sk + bk + j));
+        }
+    }
+}
+
+// Global slot cursors of the second walk (used by rows listed in place):
 // role A at off[e], role B at off[e] + cA[e].
 __global__ void list_cursor_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ cA, int64_t E,
                                    unsigned long long* __restrict__ curA, unsigned long long* __restrict__ curB,
                                    const PeelCtl* ctl) {
-    if (*(volatile const int*)&ctl->list_skip) return;
+    if (*(volatile const int*)&ctl->rewalk_skip) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
         const unsigned long long o = (unsigned long long)off[e];
@@ -1052,7 +1180,7 @@ __global__ void ktruss_out_kernel(const int2* __restrict__ es, int64_t E, uint8_
 
 __global__ void stats_final_kernel(PeelCtl* ctl, int64_t* stats, int mode) {
     stats[TDT_STAT_STATUS] = ctl->g.status;
-    stats[TDT_STAT_LISTED] = ctl->listed;
+    stats[TDT_STAT_LISTED] = ctl->listed ? (ctl->compact_skip ? 1 : 2) : 0;
     if (mode != 0) {
         stats[TDT_STAT_ALIVE] = (long long)ctl->alive;
         stats[TDT_STAT_ROUNDS] = ctl->rounds;
@@ -1116,6 +1244,10 @@ int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int6
                         const int32_t* cA, const int32_t* cB, unsigned long long* curA_g,
                         unsigned long long* curB_g, int2* lists, void* ctl, const int* gate, int* status,
                         cudaStream_t st);
+int launch_support_stage(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* soff,
+                         const int32_t* bnd, int32_t* cA, int32_t* cB, int32_t* cC, unsigned long long* curA_g,
+                         unsigned long long* curB_g, int2* stage_end, unsigned long long stage_slots, void* ctl,
+                         const int* gate, int* status, cudaStream_t st);
 int launch_list_transpose(const int64_t* cp, const int32_t* in_eid, int64_t nv, int64_t ne, const int64_t* off,
                           const int32_t* cA, const int32_t* cB, int2* lists, unsigned long long* cur, void* next,
                           const int* gate, int* status, cudaStream_t st);
@@ -1144,10 +1276,13 @@ struct Layout {
     int32_t* sup;
     int2* es;
     int32_t* round_level;
-    int4* qi[2];
-    long long* qb[2];
+    int4* qi[3];
+    long long* qb[3];
     int64_t* off;
+    int64_t* soff;
+    int32_t* bnd;
     int32_t* alive[2];
+    unsigned* dead;
     void* scan_ws;
     void* sort_ws;
     size_t total;
@@ -1167,13 +1302,16 @@ Layout carve(void* ws, int64_t V, int64_t E) {
     L.sup = (int32_t*)c.take(4 * e);
     L.es = (int2*)c.take(8 * e);
     L.round_level = (int32_t*)c.take(4 * (e + 2));
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < 3; b++) {
         L.qi[b] = (int4*)c.take(16 * e);
         L.qb[b] = (long long*)c.take(8 * e);
     }
     L.off = (int64_t*)c.take(8 * (e + 1));
+    L.soff = (int64_t*)c.take(8 * (e + 1));
+    L.bnd = (int32_t*)c.take(4 * e);
     L.alive[0] = (int32_t*)c.take(4 * e);
     L.alive[1] = (int32_t*)c.take(4 * e);
+    L.dead = (unsigned*)c.take(4 * (e / 32 + 1));
     size_t scan_b = scan_scratch_bytes((int64_t)(e > v ? e : v) + 1);
     L.scan_ws = c.take(scan_b);
     L.sort_ws = c.take(radix_sort_scratch_bytes((int64_t)e));
@@ -1227,42 +1365,35 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     }
     validate_kernel<<<g_e, tb, 0, st>>>(rp, rows_use, cols, E, V, L.ctl);
     TDT_LAUNCH_CHECK("validate");
-    // pass 1: support role counts (skipped on the device when validation failed);
-    // cA, cB, cC live in the first queue buffer until the peel starts
+    // cA, cB, cC (role counts) live in the first queue buffer until the peel starts
     int32_t* cA = reinterpret_cast<int32_t*>(L.qi[0]);
     int32_t* cB = cA + E;
     int32_t* cC = cB + E;
     prof_mark(0, st);
-    rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->g.status, st);
-    if (rc) return rc;
-    init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
-    TDT_LAUNCH_CHECK("init_state");
-    prof_mark(1, st);
+    TDT_CUDA(cudaMemsetAsync(cA, 0, 12 * (size_t)E, st));
     if (mode == 2) {
+        // triangle count: the count-only walk (skipped on the device when
+        // validation failed)
+        rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->g.status, st);
+        if (rc) return rc;
+        init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
+        TDT_LAUNCH_CHECK("init_state");
+        prof_mark(1, st);
         if (support_out) TDT_CUDA(cudaMemcpyAsync(support_out, L.sup, 4 * (size_t)E, cudaMemcpyDeviceToDevice, st));
         stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 1);
         TDT_LAUNCH_CHECK("stats_final");
         for (int ph = 2; ph <= 4; ph++) prof_mark(ph, st);
         return TDT_OK;
     }
-    // pass 2: per-edge triangle lists in the workspace tail when 24 T bytes fit
-    rc = exclusive_scan<int32_t, int64_t>(L.sup, L.off, E, L.off + E, L.scan_ws, st);
-    if (rc) return rc;
+    // The list tail: final lists grow from its start, the one walk's staging
+    // area (indexed backwards) ends at its end.
     const size_t list_base = (need + 255) & ~(size_t)255;
     const unsigned long long tail = ws_bytes > list_base ? (unsigned long long)(ws_bytes - list_base) : 0ull;
     int2* lists = reinterpret_cast<int2*>(reinterpret_cast<char*>(ws) + list_base);
-    list_decide_kernel<<<1, 1, 0, st>>>(L.off, E, tail, tail > 0, L.ctl);
-    TDT_LAUNCH_CHECK("list_decide");
-    unsigned long long* curA = reinterpret_cast<unsigned long long*>(L.qb[0]);
-    unsigned long long* curB = reinterpret_cast<unsigned long long*>(L.qb[1]);
-    list_cursor_kernel<<<g_e, tb, 0, st>>>(L.off, cA, E, curA, curB, L.ctl);
-    TDT_LAUNCH_CHECK("list_cursor");
-    // roles A and B (the listing pass checks its own counts per row)
-    rc = launch_support_list(rp, cols, V, E, L.off, cA, cB, curA, curB, lists, L.sup_ctl, &L.ctl->list_skip,
-                             &L.ctl->g.status, st);
-    if (rc) return rc;
-    // in-adjacency (CSC) of the oriented graph: role-C transpose, and the peel
-    // without lists
+    const unsigned long long stage_slots = tail / 8;
+    int2* stage_end = lists + stage_slots;
+    // in-adjacency (CSC) of the oriented graph: staging bounds, role-C
+    // transpose, and the peel without lists
     TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
     indeg_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.indeg, L.ctl);
     TDT_LAUNCH_CHECK("indeg");
@@ -1271,6 +1402,42 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     TDT_CUDA(cudaMemsetAsync(L.indeg, 0, 4 * (size_t)V, st));
     csc_fill_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, E, V, L.cp, L.indeg, L.in_src, L.in_eid, L.ctl);
     TDT_LAUNCH_CHECK("csc_fill");
+    // staging regions of the one walk (L.sup holds their sizes until
+    // init_state overwrites it), and the choice of walk
+    stage_bounds_kernel<<<g_e, tb, 0, st>>>(rows_use, cols, rp, L.cp, E, L.bnd, L.sup, L.ctl);
+    TDT_LAUNCH_CHECK("stage_bounds");
+    rc = exclusive_scan<int32_t, int64_t>(L.sup, L.soff, E, L.soff + E, L.scan_ws, st);
+    if (rc) return rc;
+    stage_decide_kernel<<<1, 1, 0, st>>>(L.soff, E, V, tail, tail > 0, L.ctl);
+    TDT_LAUNCH_CHECK("stage_decide");
+    unsigned long long* curA = reinterpret_cast<unsigned long long*>(L.qb[0]);
+    unsigned long long* curB = reinterpret_cast<unsigned long long*>(L.qb[1]);
+    stage_cursor_kernel<<<g_e, tb, 0, st>>>(L.soff, L.bnd, E, curA, curB, L.ctl);
+    TDT_LAUNCH_CHECK("stage_cursor");
+    // the walk: counts and staged role-A/B entries, or counts only (each
+    // launch returns at once when its gate is set)
+    rc = launch_support_stage(rp, cols, V, E, L.soff, L.bnd, cA, cB, cC, curA, curB, stage_end, stage_slots,
+                              L.sup_ctl, &L.ctl->stage_skip, &L.ctl->g.status, st);
+    if (rc) return rc;
+    rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->roles_skip, st);
+    if (rc) return rc;
+    init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
+    TDT_LAUNCH_CHECK("init_state");
+    prof_mark(1, st);
+    // per-edge triangle lists in the workspace tail when 24 T bytes fit
+    rc = exclusive_scan<int32_t, int64_t>(L.sup, L.off, E, L.off + E, L.scan_ws, st);
+    if (rc) return rc;
+    list_decide_kernel<<<1, 1, 0, st>>>(L.off, L.soff, E, tail, tail > 0, L.ctl);
+    TDT_LAUNCH_CHECK("list_decide");
+    stage_compact_kernel<<<grid_for(E * 32, tb, di.sms, 8), tb, 0, st>>>(L.soff, L.bnd, cA, cB, L.off, stage_end,
+                                                                           lists, E, L.ctl);
+    TDT_LAUNCH_CHECK("stage_compact");
+    // second walk, when the lists fit but not beside the staging area
+    list_cursor_kernel<<<g_e, tb, 0, st>>>(L.off, cA, E, curA, curB, L.ctl);
+    TDT_LAUNCH_CHECK("list_cursor");
+    rc = launch_support_list(rp, cols, V, E, L.off, cA, cB, curA, curB, lists, L.sup_ctl, &L.ctl->rewalk_skip,
+                             &L.ctl->g.status, st);
+    if (rc) return rc;
     // role C of every list, from the role-A lists of each vertex's in-edges
     rc = launch_list_transpose(L.cp, L.in_eid, V, E, L.off, cA, cB, lists,
                                reinterpret_cast<unsigned long long*>(L.qi[1]), L.sup_ctl, &L.ctl->list_skip,
@@ -1288,7 +1455,12 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     PeelArgs A;
     A.rp = rp; A.cols = cols; A.rows = rows_use; A.cp = L.cp; A.in_src = L.in_src; A.in_eid = L.in_eid;
     A.es = L.es; A.round_level = L.round_level;
-    A.qi[0] = L.qi[0]; A.qi[1] = L.qi[1]; A.qb[0] = L.qb[0]; A.qb[1] = L.qb[1];
+    for (int b = 0; b < 3; b++) {
+        A.qi[b] = L.qi[b];
+        A.qb[b] = L.qb[b];
+    }
+    A.dead = L.dead;
+    TDT_CUDA(cudaMemsetAsync(L.dead, 0, 4 * (size_t)(E / 32 + 1), st));
     A.off = L.off; A.lists = lists;
     A.alive[0] = L.alive[0]; A.alive[1] = L.alive[1];
     A.V = V; A.E = E; A.round_cap = E + 2;

@@ -35,6 +35,13 @@
 //              row's counters in shared memory; both edges are in the source
 //              row, so the stores stay in that row's list region); role C is
 //              filled afterwards from the role-A lists (transpose.cu).
+//   kSupStage  one walk for counts and lists: the role counts of kSupRoles,
+//              and every triangle's role-A and role-B entries written into a
+//              staging region per edge whose size is an upper bound known
+//              before the walk (role A of (u,v), v = N+(u)[i]: at most
+//              min(d+(u)-i-1, d+(v)); role B of (u,w), w = N+(u)[p]: at most
+//              min(p, d-(w)-1)); a compaction pass then packs them into the
+//              final lists.  Saves the second walk of kSupList.
 #include "common.cuh"
 
 namespace tdt {
@@ -78,7 +85,7 @@ static_assert(kHeavyCap >= 4096, "heavy cap");
 static_assert((1 << kHugeBmLog2) / 8 <= kHvS, "in-place bitmap");
 static_assert(kHeavyCap < 65536, "packed 16-bit role counters");
 
-enum SupMode { kSupAccum = 0, kSupRoles = 1, kSupList = 2 };
+enum SupMode { kSupAccum = 0, kSupRoles = 1, kSupList = 2, kSupStage = 3 };
 
 // Row ranges are clamped to [0, ne] so a malformed row_ptr cannot move an
 // access outside cols/out.
@@ -105,9 +112,13 @@ struct SupArgs {
     const int64_t* off;             // kSupList: list offsets int64[E+1]
     const int32_t* cA_in;           // kSupList: role-A counts (role-B base = off + cA)
     const int32_t* cB_in;           // kSupList: role-B counts (end-of-row check)
-    unsigned long long* curA_g;     // kSupList: global cursors for rows searched in place
+    unsigned long long* curA_g;     // kSupList / kSupStage: global cursors for rows searched in place
     unsigned long long* curB_g;
-    int2* lists;
+    int2* lists;                    // kSupList: final lists; kSupStage: one past the end of the
+                                    // staging area, which is indexed backwards (slot s at lists[-1-s])
+    const int64_t* soff;            // kSupStage: staging offsets int64[E+1]
+    const int32_t* bnd;             // kSupStage: role-A bound per edge (role-B region follows it)
+    unsigned long long stage_cap;   // kSupStage: slots the staging area holds; no store at or past it
     const int* gate;                // non-zero: skip the pass
     int* status;                    // kSupList: set when a row's slots do not end where counted
     int warp_cap;                   // rows with d+ <= warp_cap go to one warp (<= kWarpCap)
@@ -117,6 +128,9 @@ struct SupArgs {
 // Test hook: lower the light/heavy thresholds so small graphs drive every path
 // (0 restores the defaults).
 static int g_warp_cap = 0, g_heavy_cap = 0;
+// Test hook: 0 forces the scalar wedge walk (the vectorised one is the default).
+static int g_vec_walk = 1;
+void set_vector_walk(int on) { g_vec_walk = on != 0; }
 void set_support_caps(int warp_cap, int heavy_cap) {
     g_warp_cap = warp_cap;
     g_heavy_cap = heavy_cap;
@@ -175,6 +189,23 @@ __device__ __forceinline__ void on_triangle(const RowState& R, const SupArgs& A,
             atomicAdd(A.cA + R.bu + i, 1);
             atomicAdd(A.cB + R.bu + p, 1);
         }
+        atomicAdd(A.cC + pos, 1);
+    } else if (M == kSupStage) {
+        const int32_t eA = (int32_t)(R.bu + i), eB = (int32_t)(R.bu + p), eC = (int32_t)pos;
+        unsigned long long sA, sB;
+        if (R.packed) {
+            const uint32_t a = atomicAdd(R.cnt + i, 1u) & 0xffffu;
+            const uint32_t b = atomicAdd(R.cnt + p, 1u << 16) >> 16;
+            sA = (unsigned long long)__ldg(A.soff + eA) + a;
+            sB = (unsigned long long)__ldg(A.soff + eB) + (unsigned long long)__ldg(A.bnd + eB) + b;
+        } else {
+            sA = atomicAdd(A.curA_g + eA, 1ull);
+            sB = atomicAdd(A.curB_g + eB, 1ull);
+        }
+        // a count past its bound is caught per row in flush_row; this check
+        // only keeps every store inside the staging area
+        if (sA < A.stage_cap) A.lists[-1 - (long long)sA] = make_int2(eB, eC);
+        if (sB < A.stage_cap) A.lists[-1 - (long long)sB] = make_int2(eA, eC);
         atomicAdd(A.cC + pos, 1);
     } else {
         const int32_t eA = (int32_t)(R.bu + i), eB = (int32_t)(R.bu + p), eC = (int32_t)pos;
@@ -282,6 +313,85 @@ __device__ __forceinline__ void walk_group(const OutRows<Off>& G, const SupArgs&
     }
 }
 
+// The same walk over 16-byte chunks of cols, four wedges per lane and step:
+// each out-list N+(v) = cols[BV[k], HI[k]) is widened to the aligned chunks
+// that hold it, so a chunk belongs to one v and comes with one int4 load; the
+// widened ends are masked by [BV[k], HI[k]).  SC[0..n) are the strictly
+// increasing chunk starts of the group's lists in the flat chunk space, c0 a
+// multiple of 32 and o0 the group entry that holds chunk c0.  One owner
+// reduction serves 128 wedges instead of 32.  cols must be 16-byte aligned
+// (a 16-byte chunk never crosses a page, so the widened reads stay mapped).
+template <int M, bool kIdOrdered, class Off>
+__device__ __forceinline__ void walk_group_vec(const OutRows<Off>& G, const SupArgs& A, const RowState& R,
+                                               const int32_t* SC, const int32_t* VI, const int32_t* BV,
+                                               const int32_t* HI, int n, int c0, int c1, int o0, WarpQueue& Q) {
+    const unsigned lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int4* __restrict__ cols4 = reinterpret_cast<const int4*>(G.cols);
+    int ob = o0;
+    for (int base = c0; base < c1; base += kWarp) {
+        const int k = ob + 1 + (int)lane;
+        const int32_t B = k < n ? SC[k] : INT32_MAX;
+        const unsigned bit = ((unsigned)(B - base) < (unsigned)kWarp) ? (1u << (B - base)) : 0u;
+        const unsigned mk = __reduce_or_sync(kFull, bit);
+        const int nb = __popc(mk);
+        const int32_t Bn = __shfl_sync(kFull, B, nb);
+        const int c = base + (int)lane;
+        unsigned cm = 0;
+        int32_t p0 = 0;
+        int vi = 0;
+        if (c < c1) {
+            const int o = ob + __popc(mk & (lt | (1u << lane)));
+            const int32_t lo = BV[o], hi = HI[o];
+            p0 = ((lo >> 2) + (c - SC[o])) << 2;
+            const int4 w4 = __ldg(cols4 + (p0 >> 2));
+            const int32_t wq[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int32_t w = wq[q];
+                if (p0 + q >= lo && p0 + q < hi && w <= R.umax) {
+                    const uint32_t h = bm_hash(w, R.bm_log2);
+                    cm |= ((R.bm[h >> 5] >> (h & 31)) & 1u) << q;
+                }
+            }
+            vi = VI[o];
+        }
+        ob += nb + (Bn == base + kWarp ? 1 : 0);
+        if (__any_sync(kFull, cm != 0)) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const bool cand = (cm >> q) & 1u;
+                const unsigned m = __ballot_sync(kFull, cand);
+                if (m == 0) continue;
+                if (cand) {
+                    const int at = Q.n + __popc(m & lt);
+                    Q.pos[at] = p0 + q;
+                    Q.vi[at] = vi;
+                }
+                Q.n += __popc(m);
+                if (Q.n >= kWarp) {
+                    __syncwarp();
+                    resolve<M, kIdOrdered>(G, A, R, Q, kWarp);
+                    __syncwarp();
+                    const int rest = Q.n - kWarp;
+                    int32_t p2 = 0, v2 = 0;
+                    if ((int)lane < rest) {
+                        p2 = Q.pos[kWarp + lane];
+                        v2 = Q.vi[kWarp + lane];
+                    }
+                    __syncwarp();
+                    if ((int)lane < rest) {
+                        Q.pos[lane] = p2;
+                        Q.vi[lane] = v2;
+                    }
+                    __syncwarp();
+                    Q.n = rest;
+                }
+            }
+        }
+    }
+}
+
 template <int M, bool kIdOrdered, class Off>
 __device__ __forceinline__ void drain(const OutRows<Off>& G, const SupArgs& A, const RowState& R, WarpQueue& Q) {
     __syncwarp();
@@ -348,6 +458,29 @@ __device__ __forceinline__ void flush_row(const RowState& R, const SupArgs& A, i
         }
         return;
     }
+    if (M == kSupStage) {
+        // role counts from the row's counters (or its cursors), each within
+        // its staging bound
+        for (int i = tid; i < d; i += nthr) {
+            const int64_t e = R.bu + i;
+            const unsigned long long o = (unsigned long long)__ldg(A.soff + e);
+            const unsigned long long bA = (unsigned long long)__ldg(A.bnd + e);
+            const unsigned long long bB = (unsigned long long)__ldg(A.soff + e + 1) - o - bA;
+            unsigned long long ca, cb;
+            if (R.packed) {
+                const uint32_t c = R.cnt[i];
+                ca = c & 0xffffu;
+                cb = c >> 16;
+            } else {
+                ca = A.curA_g[e] - o;
+                cb = A.curB_g[e] - o - bA;
+            }
+            A.cA[e] = (int32_t)ca;
+            A.cB[e] = (int32_t)cb;
+            if ((ca > bA || cb > bB) && A.status) atomicMax(A.status, (int)TDT_ERR_CAPACITY);
+        }
+        return;
+    }
     if (!R.packed) return;
     if (M == kSupAccum) {
         for (int i = tid; i < d; i += nthr)
@@ -364,7 +497,8 @@ __device__ __forceinline__ void flush_row(const RowState& R, const SupArgs& A, i
 
 // ctl != nullptr: dynamic scheduling through its counters (zeroed by the
 // caller); ctl == nullptr: static round-robin scheduling (no scratch at all).
-template <int M, bool kIdOrdered, class Off>
+// kVec: the wedge walk loads 16-byte chunks of cols (walk_group_vec).
+template <int M, bool kIdOrdered, bool kVec, class Off>
 __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRows<Off> G, SupArgs A, SupCtl* ctl) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int32_t s_list[kHeavyChunk];
@@ -386,6 +520,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
         int32_t* g_S = reinterpret_cast<int32_t*>(smem + kHvS);
         int32_t* g_VI = reinterpret_cast<int32_t*>(smem + kHvVI);
         int32_t* g_BV = reinterpret_cast<int32_t*>(smem + kHvBV);
+        int32_t* g_HI = g_BV + kSeg;  // list ends (the vectorised walk)
         WarpQueue Q;
         Q.pos = reinterpret_cast<int32_t*>(smem + kHvQueues + wib * 8 * kQueue);
         Q.vi = Q.pos + kQueue;
@@ -427,8 +562,10 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                             len = (int32_t)(G.end(v) - bv);
                         }
                     }
+                    // work units of the walk: wedges, or 16-byte chunks of cols
+                    const int32_t units = kVec ? (len > 0 ? ((bv + len + 3) >> 2) - (bv >> 2) : 0) : len;
                     const unsigned nem = __ballot_sync(kFull, len > 0);
-                    const int32_t incl = warp_incl_scan(len);
+                    const int32_t incl = warp_incl_scan(units);
                     if (lane == 31) {
                         s_wsum[0][wib] = incl;
                         s_wsum[1][wib] = __popc(nem);
@@ -450,9 +587,10 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                     __syncthreads();
                     if (len > 0) {
                         const int ci = s_wsum[1][wib] + __popc(nem & lanemask_lt());
-                        g_S[ci] = s_wsum[0][wib] + incl - len;
+                        g_S[ci] = s_wsum[0][wib] + incl - units;
                         g_VI[ci] = i;
                         g_BV[ci] = bv;
+                        g_HI[ci] = bv + len;
                     }
                     const int total = s_wsum[0][kSupWarps];
                     const int n = s_wsum[1][kSupWarps];
@@ -472,7 +610,8 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                             o0 = lo;
                         }
                         o0 = __shfl_sync(kFull, o0, 0);
-                        walk_group<M, kIdOrdered>(G, A, R, g_S, g_VI, g_BV, n, w0, w1, o0, Q);
+                        if (kVec) walk_group_vec<M, kIdOrdered>(G, A, R, g_S, g_VI, g_BV, g_HI, n, w0, w1, o0, Q);
+                        else walk_group<M, kIdOrdered>(G, A, R, g_S, g_VI, g_BV, n, w0, w1, o0, Q);
                     }
                     __syncthreads();  // the group arrays are rewritten next
                 }
@@ -492,6 +631,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
     int32_t* l_S = reinterpret_cast<int32_t*>(sl + kSlS);
     int32_t* l_VI = reinterpret_cast<int32_t*>(sl + kSlVI);
     int32_t* l_BV = reinterpret_cast<int32_t*>(sl + kSlBV);
+    int32_t* l_HI = l_BV + kWarp;  // list ends (the vectorised walk)
     uint32_t* l_bm = reinterpret_cast<uint32_t*>(sl + kSlBm);
     WarpQueue Q;
     Q.pos = reinterpret_cast<int32_t*>(sl + kSlQ);
@@ -535,17 +675,22 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                         len = (int32_t)(G.end(v) - bv);
                     }
                 }
+                const int32_t units = kVec ? (len > 0 ? ((bv + len + 3) >> 2) - (bv >> 2) : 0) : len;
                 const unsigned nem = __ballot_sync(kFull, len > 0);
-                const int32_t incl = warp_incl_scan(len);
+                const int32_t incl = warp_incl_scan(units);
                 const int total = __shfl_sync(kFull, incl, 31);
                 if (len > 0) {
                     const int ci = __popc(nem & lanemask_lt());
-                    l_S[ci] = incl - len;
+                    l_S[ci] = incl - units;
                     l_VI[ci] = i;
                     l_BV[ci] = bv;
+                    l_HI[ci] = bv + len;
                 }
                 __syncwarp();
-                if (total > 0) walk_group<M, kIdOrdered>(G, A, R, l_S, l_VI, l_BV, __popc(nem), 0, total, 0, Q);
+                if (total > 0) {
+                    if (kVec) walk_group_vec<M, kIdOrdered>(G, A, R, l_S, l_VI, l_BV, l_HI, __popc(nem), 0, total, 0, Q);
+                    else walk_group<M, kIdOrdered>(G, A, R, l_S, l_VI, l_BV, __popc(nem), 0, total, 0, Q);
+                }
                 __syncwarp();
             }
             drain<M, kIdOrdered>(G, A, R, Q);
@@ -563,7 +708,10 @@ static int launch_mode(const OutRows<Off>& G, const SupArgs& A, SupCtl* ctl, cud
     SupArgs A2 = A;
     A2.warp_cap = (g_warp_cap > 0 && g_warp_cap < kWarpCap) ? g_warp_cap : kWarpCap;
     A2.heavy_cap = (g_heavy_cap > 0 && g_heavy_cap < kHeavyCap) ? g_heavy_cap : kHeavyCap;
-    auto kern = support_kernel<M, kIdOrdered, Off>;
+    // the vectorised walk needs 16-byte aligned columns (chunk positions stay
+    // below 2^31 under 2^30 edges)
+    const bool vec = g_vec_walk && ((uintptr_t)G.cols & 15u) == 0 && G.ne < (1ll << 30);
+    auto kern = vec ? support_kernel<M, kIdOrdered, true, Off> : support_kernel<M, kIdOrdered, false, Off>;
     TDT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSupSmemBytes));
     TDT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     if (ctl) TDT_CUDA(cudaMemsetAsync(ctl, 0, sizeof(SupCtl), st));
@@ -585,13 +733,11 @@ int launch_support_accum_i32(const int32_t* rp, int32_t stride, const int32_t* c
     return launch_mode<kSupAccum, false, int32_t>(G, A, nullptr, st);
 }
 
-// Whole-path pass 1: role counts.  cA/cB are stored per row, cC accumulated by
-// atomics, so all three are zeroed first.
+// Whole-path count-only walk: role counts.  cA/cB are stored per row (by
+// atomics for rows searched in place), cC accumulated by atomics: the caller
+// zeroes all three first.
 int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* cA, int32_t* cB,
                          int32_t* cC, void* ctl, const int* gate, cudaStream_t st) {
-    TDT_CUDA(cudaMemsetAsync(cA, 0, 4 * (size_t)ne, st));
-    TDT_CUDA(cudaMemsetAsync(cB, 0, 4 * (size_t)ne, st));
-    TDT_CUDA(cudaMemsetAsync(cC, 0, 4 * (size_t)ne, st));
     if (nv <= 0) return TDT_OK;
     OutRows<int64_t> G{rp, 1, cols, nv, ne};
     SupArgs A{};
@@ -618,6 +764,30 @@ int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int6
     A.gate = gate;
     A.status = status;
     return launch_mode<kSupList, true, int64_t>(G, A, reinterpret_cast<SupCtl*>(ctl), st);
+}
+
+// Whole-path one-walk pass: role counts (cA, cB stored per row, cC by
+// atomics: the caller zeroes cC first) and the role-A/B entries of every
+// triangle in the staging regions (skipped on the device when *gate != 0).
+int launch_support_stage(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* soff,
+                         const int32_t* bnd, int32_t* cA, int32_t* cB, int32_t* cC, unsigned long long* curA_g,
+                         unsigned long long* curB_g, int2* stage_end, unsigned long long stage_slots, void* ctl,
+                         const int* gate, int* status, cudaStream_t st) {
+    if (nv <= 0) return TDT_OK;
+    OutRows<int64_t> G{rp, 1, cols, nv, ne};
+    SupArgs A{};
+    A.cA = cA;
+    A.cB = cB;
+    A.cC = cC;
+    A.soff = soff;
+    A.bnd = bnd;
+    A.curA_g = curA_g;
+    A.curB_g = curB_g;
+    A.lists = stage_end;
+    A.gate = gate;
+    A.status = status;
+    A.stage_cap = stage_slots;
+    return launch_mode<kSupStage, true, int64_t>(G, A, reinterpret_cast<SupCtl*>(ctl), st);
 }
 
 size_t support_ctl_bytes() { return 256; }

@@ -26,6 +26,7 @@ class TrussResult(NamedTuple):
     triangles: int
     rounds: int
     listed: bool = False      # the peel read per-edge triangle lists (else it searched)
+    listing: int = 0          # 0 search peel; lists written by 1 a second walk, 2 the one walk
 
 
 class Workspace:
@@ -51,13 +52,39 @@ def _graph_key(cols, rp):
 
 
 LIST_BUDGET_FRACTION = 0.6
+# lists plus the one walk's staging area (which is dead memory once the lists
+# are packed) may take more of the free memory
+STAGE_BUDGET_FRACTION = 0.75
 
 
-def _list_bytes(ws, cols, rp, lists, base):
-    """Bytes for the per-edge triangle lists (24 per triangle), or 0 to let
-    the peel search the adjacency instead.  lists: True/False/"auto" ("auto"
-    keeps lists whenever they fit: the listed peel is the faster one at every
-    size, from 10 K edges up)."""
+def stage_bytes(cols, rp, rows=None):
+    """Bytes of the one-walk pass's staging area: 8 per slot of the role-A /
+    role-B bounds of every edge e = (u, v) at position i of row u:
+    min(d+(u) - i - 1, d+(v)) + min(i, d-(v) - 1), the bounds the device
+    computes (stage_bounds_kernel)."""
+    rp = rp.to(torch.int64)
+    V, E = rp.shape[0] - 1, cols.shape[0]
+    if E == 0:
+        return 0
+    dplus = rp[1:] - rp[:-1]
+    if rows is None:
+        rows = torch.repeat_interleave(torch.arange(V, device=cols.device), dplus)
+    u = rows.to(torch.int64)
+    v = cols.to(torch.int64)
+    i = torch.arange(E, device=cols.device) - rp[u]
+    indeg = torch.bincount(v, minlength=V)
+    a = torch.minimum(dplus[u] - i - 1, dplus[v]).clamp_min_(0)
+    b = torch.minimum(i, indeg[v] - 1).clamp_min_(0)
+    return 8 * int((a + b).sum())
+
+
+def _list_bytes(ws, cols, rp, lists, base, rows=None):
+    """Bytes for the workspace's list tail, or 0 to let the peel search the
+    adjacency instead: the per-edge triangle lists (24 bytes per triangle)
+    plus, when that fits too, the staging area of the one-walk pass (which
+    then counts and lists in one walk instead of two).  lists:
+    True/False/"auto" ("auto" keeps lists whenever they fit: the listed peel
+    is the faster one at every size, from 10 K edges up)."""
     if lists is False:
         return 0
     key = _graph_key(cols, rp)
@@ -65,11 +92,18 @@ def _list_bytes(ws, cols, rp, lists, base):
     if T is None:
         T = triangle_count_arrays(cols, rp, ws)
         ws.triangles[key] = T
+    sk = ("stage",) + key
+    S = ws.triangles.get(sk)
+    if S is None:
+        S = stage_bytes(cols, rp, rows)
+        ws.triangles[sk] = S
     need = 24 * T + 256
     if lists is True:
-        return need
+        return need + S
     free, _ = torch.cuda.mem_get_info(cols.device)
     have = free + (ws.buf.numel() if ws.buf is not None else 0) - base
+    if need + S <= STAGE_BUDGET_FRACTION * have:
+        return need + S
     return need if need <= LIST_BUDGET_FRACTION * have else 0
 
 
@@ -128,7 +162,7 @@ def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto",
     need = L.tdt_decompose_workspace_bytes(V, E)
     wso = _ws_for(dev, workspace)
     base = (need + 255) // 256 * 256
-    tail = int(list_budget) if list_budget is not None else _list_bytes(wso, cols, rp, lists, base)
+    tail = int(list_budget) if list_budget is not None else _list_bytes(wso, cols, rp, lists, base, rows)
     ws = wso.get(base + tail)
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
     # pass the requested size, not the (possibly larger, shared) buffer: the
@@ -143,7 +177,7 @@ def truss_decompose(graph, workspace=None, stream=None, sync=True, lists="auto",
     sh = stats.cpu()
     _check_stats(sh, "tdt_truss_decompose")
     return TrussResult(truss, e_truss[: int(sh[STAT_NETRUSS])], ptr[: int(sh[STAT_NPTR])], int(sh[STAT_KMAX]),
-                       int(sh[STAT_TRIANGLES]), int(sh[STAT_ROUNDS]), bool(sh[STAT_LISTED]))
+                       int(sh[STAT_TRIANGLES]), int(sh[STAT_ROUNDS]), bool(sh[STAT_LISTED]), int(sh[STAT_LISTED]))
 
 
 def ktruss_search(graph, k, workspace=None, stream=None, lists="auto"):
@@ -157,7 +191,7 @@ def ktruss_search(graph, k, workspace=None, stream=None, lists="auto"):
     stats = torch.zeros(STAT_COUNT, dtype=torch.int64, device=dev)
     wso = _ws_for(dev, workspace)
     base = (L.tdt_decompose_workspace_bytes(V, E) + 255) // 256 * 256
-    tail = _list_bytes(wso, cols, rp, lists, base)
+    tail = _list_bytes(wso, cols, rp, lists, base, rows)
     ws = wso.get(base + tail)
     s = (stream or torch.cuda.current_stream(dev)).cuda_stream
     with torch.cuda.device(cols.device):

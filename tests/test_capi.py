@@ -62,3 +62,9 @@ def test_workspace_query_is_pure_host(lib):
 
 def test_built_for_sm103a_only():
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_noalloc_scratch_holds_its_size_limit(lib):
+    """tdt_triangle_count_noalloc accepts graphs up to 2^18 vertices and 2^18
+    edges; the workspace of that corner must fit its fixed 40 MiB scratch."""
+    assert lib.tdt_decompose_workspace_bytes(1 << 18, 1 << 18) <= 40 << 20

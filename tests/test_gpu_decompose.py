@@ -160,10 +160,12 @@ def test_repeatable_and_workspace_reuse():
     assert torch.equal(a.truss, b.truss) and torch.equal(a.e_truss, b.e_truss)
 
 
+@pytest.mark.parametrize("vec", [1, 0])
 @pytest.mark.parametrize("caps", [(4, 16), (8, 10 ** 6), (2, 3)])
-def test_all_support_paths_vs_oracle(caps):
+def test_all_support_paths_vs_oracle(caps, vec):
     """Lowered light/heavy thresholds push small graphs through the block-level
-    heavy-row walk and the in-place (beyond shared memory) path."""
+    heavy-row walk and the in-place (beyond shared memory) path, with the
+    wedge walk over 16-byte column chunks and over single columns."""
     from tdtdecomposition_gb300 import _lib
     L = _lib.load()
     s, d = G.rmat_edges(12, 16 << 12, seed=31)
@@ -171,6 +173,7 @@ def test_all_support_paths_vs_oracle(caps):
     rows, cols, rp, verts = O.preprocess(pairs)
     sup_ref = O.support(rows, cols, rp.astype(np.int32), 1)
     L.tdt_set_support_caps(*caps)
+    L.tdt_set_vector_walk(vec)
     try:
         t, sup = T.triangle_count(graph_of(rows, cols, rp), return_support=True)
         assert np.array_equal(sup.cpu().numpy(), sup_ref)
@@ -183,6 +186,49 @@ def test_all_support_paths_vs_oracle(caps):
         assert np.array_equal(out.cpu().numpy(), sup_ref)
     finally:
         L.tdt_set_support_caps(0, 0)
+        L.tdt_set_vector_walk(1)
+
+
+def test_unaligned_columns_take_the_scalar_walk():
+    """The drop-in operator on a columns array that starts 4 bytes past a
+    16-byte boundary (the vectorised walk needs 16-byte alignment) gives the
+    oracle's support."""
+    from tdtdecomposition_gb300 import trusstensor as tt
+    s, d = G.rmat_edges(11, 16 << 11, seed=8)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, d], 1))
+    sup_ref = O.support(rows, cols, rp.astype(np.int32), 1)
+    buf = torch.zeros(len(cols) + 1, dtype=torch.int32, device="cuda")
+    buf[1:] = torch.as_tensor(cols).cuda()
+    c1 = buf[1:]
+    assert c1.data_ptr() % 16 != 0
+    out = torch.zeros(len(cols), dtype=torch.int32, device="cuda")
+    tt.segment_isin2(torch.as_tensor(rows).cuda(), c1, torch.as_tensor(rp.astype(np.int32)).cuda(), out)
+    assert np.array_equal(out.cpu().numpy(), sup_ref)
+
+
+@pytest.mark.parametrize("route", [2, 1, 0])
+def test_listing_routes_vs_oracle(route):
+    """The three ways the peel gets each edge's triangles, chosen by the list
+    tail: one walk that counts and lists (tail = lists + staging), a count
+    walk then a listing walk (tail = lists only), and the search peel (no
+    tail).  All three give the oracle's e_truss / ptr_truss."""
+    s, d = G.rmat_edges(13, 16 << 13, seed=12)
+    pairs = np.stack([s, d], 1)
+    rows, cols, rp, verts = O.preprocess(pairs)
+    V = len(verts)
+    kmax, et, pt, truss = O.k_truss(rows, cols, O.tiling_row_ptr(rows, cols, V, 1), V, 1)
+    g = graph_of(rows, cols, rp)
+    tri = T.triangle_count(g)
+    stage = T.stage_bytes(g.columns, g.row_ptr, g.rows)
+    budget = {2: 24 * tri + stage + 256, 1: 24 * tri + 256, 0: 0}[route]
+    res = T.truss_decompose(g, list_budget=budget)
+    assert res.listing == route
+    assert res.kmax == kmax
+    assert np.array_equal(res.truss.cpu().numpy(), truss)
+    assert np.array_equal(res.e_truss.cpu().numpy(), et)
+    assert np.array_equal(res.ptr_truss.cpu().numpy(), pt)
+    ks = T.ktruss_search(g, max(3, kmax // 2), lists=True)
+    assert np.array_equal(ks.cpu().numpy(), truss >= max(3, kmax // 2))
 
 
 def test_deterministic_at_scale():

@@ -19,11 +19,18 @@ pytestmark = pytest.mark.gpu
 
 
 def _graphs():
+    """(rows, cols, row_ptr, expected support or None): the golden R-MAT
+    scale-10 graph with the reference's own support, a scale-13 R-MAT graph,
+    and the size limit's corner: 2^18 edges over about 227 K vertices."""
     d = GD.load("rmat_s10")
-    yield d["ref_rows"], d["ref_cols"], d["ref_rp"]
+    yield d["ref_rows"], d["ref_cols"], d["ref_rp"], d["ref_support"]
     s, t = G.rmat_edges(13, 16 << 13, seed=5)
     rows, cols, rp, verts = O.preprocess(np.stack([s, t], 1))
-    yield rows, cols, rp
+    yield rows, cols, rp, None
+    s, t = G.er_edges(1 << 18, 1 << 18, seed=3)
+    rows, cols, rp, verts = O.preprocess(np.stack([s, t], 1))
+    assert len(cols) == 1 << 18 and len(verts) > 200000
+    yield rows, cols, rp, None
 
 
 def _count_with_workspace(L, cols, rp, stream):
@@ -41,12 +48,14 @@ def _count_with_workspace(L, cols, rp, stream):
 def test_noalloc_matches_workspace_entry_point_twice():
     L = _lib.load()
     stream = torch.cuda.current_stream().cuda_stream
-    for rows, cols_np, rp_np in _graphs():
+    for rows, cols_np, rp_np, golden in _graphs():
         cols = torch.as_tensor(cols_np, dtype=torch.int32).cuda()
         rp = torch.as_tensor(np.asarray(rp_np), dtype=torch.int64).cuda()
         V, E = rp.numel() - 1, cols.numel()
         ref_sup, ref_stats = _count_with_workspace(L, cols, rp, stream)
         assert int(ref_stats[0]) == 0
+        if golden is not None:
+            assert np.array_equal(ref_sup.numpy(), golden)
         for _ in range(2):
             sup = torch.full((E,), -7, dtype=torch.int32, device="cuda")
             stats = torch.full((8,), -1, dtype=torch.int64, device="cuda")
