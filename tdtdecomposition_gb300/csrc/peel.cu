@@ -355,6 +355,11 @@ static_assert(kDynChunk % 64 == 0, "dynamic ranges are whole 64-slot steps");
 #define TDT_SKIP_MARKED 1
 #endif
 constexpr bool kSkipMarked = TDT_SKIP_MARKED != 0;
+// The 1-bit dead-edge filter before the edge-state loads of a slot.
+#ifndef TDT_DEAD_FILTER
+#define TDT_DEAD_FILTER 1
+#endif
+constexpr bool kDeadFilter = TDT_DEAD_FILTER != 0;
 
 #ifndef TDT_PEEL_STEP
 #define TDT_PEEL_STEP 8
@@ -662,7 +667,7 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
         f = __ldg(A.in_eid + kk);
     }
     if (w == y) return false;
-    if ((A.dead[f >> 5] >> (f & 31)) & 1u) return false;  // (x,w) peeled before this round
+    if (kDeadFilter && ((A.dead[f >> 5] >> (f & 31)) & 1u)) return false;  // (x,w) peeled before this round
     const int64_t gg = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
                                : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
     g = (int32_t)gg;
@@ -693,7 +698,7 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     const int4* __restrict__ qi = A.qi[buf];
     // the edges of round r-1 are dead from this round on: set their bits (a
     // bit read before it is set only sends that triangle to the state check)
-    if (r > 0) {
+    if (kDeadFilter && r > 0) {
         long long nprev = (long long)(ld_cg_u64(&A.ctl->q[(r - 1) & 3]) >> kCandBits);
         if (nprev > A.E) nprev = A.E;
         const int4* __restrict__ qp = A.qi[(r - 1) % 3];
@@ -752,7 +757,7 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         if (va) tra = slot_edges<Listed>(A, ita, ta - wa.base_l, fa, ga);
         if (vb) trb = slot_edges<Listed>(A, itb, tb - wb.base_l, fb, gb);
         // dead-bit filter: a triangle with an edge peeled before round r is gone
-        {
+        if (kDeadFilter) {
             unsigned xa = 0, ya = 0, xb = 0, yb = 0;
             if (tra) {
                 xa = A.dead[fa >> 5];
@@ -1054,8 +1059,10 @@ __global__ void list_decide_kernel(const int64_t* __restrict__ off, const int64_
 
 // Pack the role-A / role-B entries of every edge from its staging region
 // (slot s at stage_end[-1-s]) into its final list: role A at off[e], role B
-// at off[e] + cA[e].  A warp takes 32 edges at a time (their offsets and
-// counts in one coalesced load each) and copies them one after the other.
+// at off[e] + cA[e].  A warp takes 32 edges at a time: their entries form one
+// flat index space (lane-held exclusive starts S), each lane finds the edge
+// of its entry by a 5-step search over S (shuffles), and four 32-entry
+// windows are copied per step so four loads per lane are in flight.
 __global__ void stage_compact_kernel(const int64_t* __restrict__ soff, const int32_t* __restrict__ bnd,
                                      const int32_t* __restrict__ cA, const int32_t* __restrict__ cB,
                                      const int64_t* __restrict__ off, const int2* __restrict__ stage_end,
@@ -1063,25 +1070,49 @@ __global__ void stage_compact_kernel(const int64_t* __restrict__ soff, const int
     if (*(volatile const int*)&ctl->compact_skip) return;
     const unsigned lane = lane_id();
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    constexpr int kWin = 4;
     for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kWarp; base < E;
          base += nw * kWarp) {
         const int64_t e = base + lane;
         int64_t so = 0, o = 0;
-        int32_t b = 0, na = 0, nb = 0;
+        int32_t b = 0, na = 0, n = 0;
         if (e < E) {
             so = soff[e];
             b = bnd[e];
             na = cA[e];
-            nb = cB[e];
+            n = na + cB[e];
             o = off[e];
         }
-        const int kn = E - base < kWarp ? (int)(E - base) : kWarp;
-        for (int k = 0; k < kn; k++) {
-            const int64_t sk = __shfl_sync(kFull, so, k), ok = __shfl_sync(kFull, o, k);
-            const int32_t bk = __shfl_sync(kFull, b, k), ak = __shfl_sync(kFull, na, k),
-                          ck = __shfl_sync(kFull, nb, k);
-            for (int j = (int)lane; j < ak; j += kWarp) lists[ok + j] = __ldcs(stage_end - 1 - (sk + j));
-            for (int j = (int)lane; j < ck; j += kWarp) lists[ok + ak + j] = __ldcs(stage_end - 1 - (sk + bk + j));
+        const int32_t incl = warp_incl_scan(n);
+        const int32_t total = __shfl_sync(kFull, incl, 31);
+        const int32_t S = incl - n;  // first flat entry of this lane's edge
+        for (int32_t tb = 0; tb < total; tb += kWin * kWarp) {
+            int2 v[kWin];
+            int64_t dst[kWin];
+#pragma unroll
+            for (int w = 0; w < kWin; w++) {
+                const int32_t t = tb + w * kWarp + (int)lane;
+                // last lane k with S_k <= t (S is non-decreasing, S_0 = 0)
+                int k = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int32_t Sc = __shfl_sync(kFull, S, k + step);
+                    if (Sc <= t) k += step;
+                }
+                const int32_t Sk = __shfl_sync(kFull, S, k), ak = __shfl_sync(kFull, na, k),
+                              bk = __shfl_sync(kFull, b, k);
+                const int64_t sk = __shfl_sync(kFull, so, k), ok = __shfl_sync(kFull, o, k);
+                const int32_t loc = t - Sk;
+                dst[w] = -1;
+                if (t < total) {
+                    const int64_t src = sk + (loc < ak ? loc : bk + (loc - ak));
+                    v[w] = __ldcs(stage_end - 1 - src);
+                    dst[w] = ok + loc;
+                }
+            }
+#pragma unroll
+            for (int w = 0; w < kWin; w++)
+                if (dst[w] >= 0) lists[dst[w]] = v[w];
         }
     }
 }
@@ -1248,7 +1279,8 @@ int launch_support_stage(const int64_t* rp, const int32_t* cols, int64_t nv, int
                          const int32_t* bnd, int32_t* cA, int32_t* cB, int32_t* cC, unsigned long long* curA_g,
                          unsigned long long* curB_g, int2* stage_end, unsigned long long stage_slots, void* ctl,
                          const int* gate, int* status, cudaStream_t st);
-int launch_list_transpose(const int64_t* cp, const int32_t* in_eid, int64_t nv, int64_t ne, const int64_t* off,
+int launch_list_transpose(const int64_t* cp, const int64_t* rp, const int32_t* cols, const int32_t* in_eid,
+                          int64_t nv, int64_t ne, const int64_t* off,
                           const int32_t* cA, const int32_t* cB, int2* lists, unsigned long long* cur, void* next,
                           const int* gate, int* status, cudaStream_t st);
 
@@ -1439,7 +1471,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
                              &L.ctl->g.status, st);
     if (rc) return rc;
     // role C of every list, from the role-A lists of each vertex's in-edges
-    rc = launch_list_transpose(L.cp, L.in_eid, V, E, L.off, cA, cB, lists,
+    rc = launch_list_transpose(L.cp, rp, cols, L.in_eid, V, E, L.off, cA, cB, lists,
                                reinterpret_cast<unsigned long long*>(L.qi[1]), L.sup_ctl, &L.ctl->list_skip,
                                &L.ctl->g.status, st);
     if (rc) return rc;

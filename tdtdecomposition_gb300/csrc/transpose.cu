@@ -22,6 +22,14 @@
 // own end per entry), and check_kernel verifies afterwards that every cursor
 // ended exactly at its edge's list end (else TDT_ERR_CAPACITY, and the lists
 // are not used).
+// The in-edges of a group have consecutive target vertices, whose out-edges
+// (the edges that receive the group's role-C entries) are one contiguous edge
+// range.  For the vertices whose in-edges all lie inside the group, the
+// cursors of up to kTrSmemCur of those out-edges are copied to shared memory
+// at the start of the group, advanced there, and written back at its end: no
+// other group touches them.  Only the entries of the group's first and last
+// vertices (shared with the neighbouring groups) and of very long out-edge
+// ranges take the global atomic.
 #include "common.cuh"
 
 namespace tdt {
@@ -29,9 +37,12 @@ namespace tdt {
 constexpr int kTrBlock = 512;
 constexpr int kTrWarps = kTrBlock / kWarp;
 constexpr int kTrMinBlocks = 3;
+constexpr int kTrSmemCur = 4096;   // out-edge cursors a group keeps in shared memory (32 KB)
 
 struct TrArgs {
     const int64_t* cp;                  // in-adjacency offsets (cp[V] = E)
+    const int64_t* rp;                  // out-adjacency offsets (rp[V] = E)
+    const int32_t* cols;                // out-adjacency targets
     const int32_t* in_eid;              // in-adjacency edge ids
     const int64_t* off;                 // list offsets
     const int32_t* cA;
@@ -52,6 +63,8 @@ __global__ void __launch_bounds__(kTrBlock, kTrMinBlocks) transpose_kernel(TrArg
     __shared__ int64_t s_BV[kTrBlock];
     __shared__ int32_t s_wsum[2][kTrWarps + 1];
     __shared__ long long s_group;
+    __shared__ unsigned long long s_cur[kTrSmemCur];
+    __shared__ long long s_lo, s_hi;  // out-edges [s_lo, s_hi) have their cursors in s_cur
     if (A.gate && *(volatile const int*)A.gate != 0) return;
     const int wib = threadIdx.x / kWarp;
     const unsigned lane = lane_id();
@@ -66,6 +79,27 @@ __global__ void __launch_bounds__(kTrBlock, kTrMinBlocks) transpose_kernel(TrArg
         __syncthreads();
         const long long grp = s_group;
         if (grp >= ngroups) break;
+        // the vertices whose in-edges all lie in [k0, k1), and their out-edges
+        if (threadIdx.x == 0) {
+            const int64_t k0 = grp * kTrBlock, k1 = k0 + kTrBlock < ne ? k0 + kTrBlock : ne;
+            long long lo = 0, hi = 0;
+            const int32_t e0 = __ldg(A.in_eid + k0), e1 = __ldg(A.in_eid + k1 - 1);
+            if (e0 >= 0 && e0 < ne && e1 >= 0 && e1 < ne) {
+                int32_t va = __ldg(A.cols + e0), vb = __ldg(A.cols + e1);
+                if (__ldg(A.cp + va) < k0) va++;          // shares its in-edges with the group before
+                if (__ldg(A.cp + vb + 1) > k1) vb--;      // ... with the group after
+                if (va <= vb) {
+                    lo = __ldg(A.rp + va);
+                    hi = __ldg(A.rp + vb + 1);
+                    if (hi - lo > kTrSmemCur) hi = lo + kTrSmemCur;
+                }
+            }
+            s_lo = lo;
+            s_hi = hi;
+        }
+        __syncthreads();
+        const long long clo = s_lo, chi = s_hi;
+        for (long long j = threadIdx.x; j < chi - clo; j += kTrBlock) s_cur[j] = A.cur[clo + j];
         // this thread's in-edge and the length / position of its role-A list
         const int64_t k = grp * kTrBlock + threadIdx.x;
         int32_t len = 0, eid = 0;
@@ -138,7 +172,9 @@ __global__ void __launch_bounds__(kTrBlock, kTrMinBlocks) transpose_kernel(TrArg
                     if (eC < 0 || eC >= ne) {
                         tr_fail(A);
                     } else {
-                        const unsigned long long slot = atomicAdd(A.cur + eC, 1ull);
+                        const unsigned long long slot = (eC >= clo && eC < chi)
+                                                            ? atomicAdd(s_cur + (eC - clo), 1ull)
+                                                            : atomicAdd(A.cur + eC, 1ull);
                         if (slot < cap) A.lists[slot] = make_int2(s_VI[o], ent.x);
                         else tr_fail(A);
                     }
@@ -147,6 +183,7 @@ __global__ void __launch_bounds__(kTrBlock, kTrMinBlocks) transpose_kernel(TrArg
             }
         }
         __syncthreads();  // the group arrays are rewritten next
+        for (long long j = threadIdx.x; j < chi - clo; j += kTrBlock) A.cur[clo + j] = s_cur[j];
     }
 }
 
@@ -168,7 +205,8 @@ __global__ void tr_check_kernel(const int64_t* __restrict__ off, int64_t E,
 
 // Role-C entries of every list (skipped on the device when *gate != 0).  cur:
 // uint64[E] scratch; next: 8 bytes of scratch.
-int launch_list_transpose(const int64_t* cp, const int32_t* in_eid, int64_t nv, int64_t ne, const int64_t* off,
+int launch_list_transpose(const int64_t* cp, const int64_t* rp, const int32_t* cols, const int32_t* in_eid,
+                          int64_t nv, int64_t ne, const int64_t* off,
                           const int32_t* cA, const int32_t* cB, int2* lists, unsigned long long* cur, void* next,
                           const int* gate, int* status, cudaStream_t st) {
     if (nv <= 0 || ne <= 0) return TDT_OK;
@@ -182,7 +220,7 @@ int launch_list_transpose(const int64_t* cp, const int32_t* in_eid, int64_t nv, 
     int per_sm = 0;
     TDT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transpose_kernel, kTrBlock, 0));
     if (per_sm < 1) per_sm = 1;
-    TrArgs A{cp, in_eid, off, cA, cur, lists, status, gate, ne};
+    TrArgs A{cp, rp, cols, in_eid, off, cA, cur, lists, status, gate, ne};
     transpose_kernel<<<di.sms * per_sm, kTrBlock, 0, st>>>(A, reinterpret_cast<unsigned long long*>(next));
     TDT_LAUNCH_CHECK("list_transpose");
     tr_check_kernel<<<g_e, 256, 0, st>>>(off, ne, cur, gate, status);
