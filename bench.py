@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-skewed", action="store_true", help="skip the Chung-Lu 2^25 section")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own GPU kernels beside this build's")
+    ap.add_argument("--no-same-scale", action="store_true",
+                    help="skip the GPU decomposition of the CPU arm's graph")
     ap.add_argument("--skewed", action="store_true",
                     help="also run the skewed Chung-Lu graph (n=2^25): triangle count, decomposition, k-truss")
     ap.add_argument("--skewed-log2n", type=int, default=25)
@@ -150,15 +155,19 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- CPU legs (oracle)
 def cpu_sample_scale(args, steps):
+    """R-MAT scale of the CPU arm for a run of `steps` decompositions (warm-up
+    included): the same in the reference arm, the cpu_baseline leg and the
+    GPU line's same_scale object of a run with the same --steps/--warmup
+    (about 10-40 s of host work on the box's 16 cores)."""
     if args.cpu_scale:
         return args.cpu_scale
-    # about 10 s of CPU work in total on the box's 16 host cores
-    return 18 if steps <= 2 else (17 if steps <= 15 else (16 if steps <= 40 else 15))
+    return 18 if steps <= 4 else (17 if steps <= 15 else (16 if steps <= 40 else 15))
 
 
 def cpu_decompose_sample(scale, reps, warm=0):
     """The oracle port of the reference's `--cuda` flow (singlegpu_truss.py
-    k_truss, OpenMP ops) on R-MAT(scale, 16*2^scale draws, seed 1)."""
+    k_truss, OpenMP ops) on R-MAT(scale, 16*2^scale draws, seed 1).  Returns
+    (E, V, seconds per run, threads, per-edge truss numbers of the last run)."""
     import numpy as np
     from oracle import oracle as O
     from tdtdecomposition_gb300 import generators as G
@@ -169,11 +178,12 @@ def cpu_decompose_sample(scale, reps, warm=0):
     for _ in range(warm):
         O.k_truss(rows, cols, rpt, V, 2)
     times = []
+    truss = None
     for _ in range(reps):
         t = time.perf_counter()
-        O.k_truss(rows, cols, rpt, V, 2)
+        truss = O.k_truss(rows, cols, rpt, V, 2)[3]
         times.append(time.perf_counter() - t)
-    return len(cols), V, times, O.num_threads()
+    return len(cols), V, times, O.num_threads(), truss
 
 
 def reference_arm(args):
@@ -183,7 +193,7 @@ def reference_arm(args):
         if rank != 0:
             return
     scale = cpu_sample_scale(args, args.steps + args.warmup)
-    E, V, times, threads = cpu_decompose_sample(scale, args.steps, args.warmup)
+    E, V, times, threads, _ = cpu_decompose_sample(scale, args.steps, args.warmup)
     t = sum(times)
     value = E * len(times) / t
     sample = "R-MAT scale %d, 16*2^%d draws, seed 1 (V=%d, E=%d), one full decomposition per step" % (
@@ -289,6 +299,7 @@ def bench_skewed(dev, log2n=25):
     from tdtdecomposition_gb300 import generators as G, truss as T
     from tdtdecomposition_gb300.preprocess import preprocess_edges
     n = 1 << log2n
+    peak = _hbm_peak()[0]
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -307,19 +318,167 @@ def bench_skewed(dev, log2n=25):
     tri, t_tc = timed(lambda: T.triangle_count(g, workspace=ws))
     res, t_dec = timed(lambda: T.truss_decompose(g, workspace=ws))
     truss = res.truss
+    # algorithmic bytes: B_sup = 4 W + 28 E + 4 (V+1); decomposition 2 B_sup;
+    # k-truss search B_sup + 4 W_del + 28 E, W_del = W over the deleted edges
+    rp = g.row_ptr.to(torch.int64)
+    dplus = rp[1:] - rp[:-1]
+    rows = g.rows if g.rows is not None else torch.repeat_interleave(torch.arange(V, device=dev), dplus)
+    wpe = dplus[rows.long()] + dplus[g.columns.long()]
+    W = int(wpe.sum())
+    B_sup = 4 * W + 28 * E + 4 * (V + 1)
+
+    def roof(B, t):
+        return {"algorithmic_bytes": B, "achieved_gbs": B / t / 1e9, "frac": B / t / 1e9 / peak}
+
     kt = {}
     for k in sorted({3, 8, res.kmax // 2, res.kmax}):
         m, tk = timed(lambda: T.ktruss_search(g, k, workspace=ws))
         if not torch.equal(m, truss >= k):
             raise SystemExit("k-truss at k=%d differs from {e : truss(e) >= k}" % k)
-        kt[str(k)] = {"edges": int(m.sum()), "s": tk, "edges_per_s": E / tk}
+        W_del = int(wpe[~m].sum())
+        kt[str(k)] = dict({"edges": int(m.sum()), "s": tk, "edges_per_s": E / tk},
+                          **roof(B_sup + 4 * W_del + 28 * E, tk))
     return {"workload": "Chung-Lu n=2^%d, exponent 2.1, mean degree 40, degree cap 2^20, seed 2" % log2n,
-            "draws": draws, "V": V, "E": E, "triangles": tri, "kmax": res.kmax, "rounds": res.rounds,
+            "draws": draws, "V": V, "E": E, "W": W, "triangles": tri, "kmax": res.kmax, "rounds": res.rounds,
             "generate_s": t_gen, "preprocess_s": t_pre, "preprocess_draws_per_s": draws / t_pre,
             "triangle_count_s": t_tc, "triangle_count_edges_per_s": E / t_tc,
-            "decompose_s": t_dec, "value": E / t_dec, "unit": UNIT,
-            "peel_mode": "lists" if res.listed else "search (24 T bytes of lists exceed the device budget)",
+            "triangle_count_roofline": roof(B_sup, t_tc),
+            "decompose_s": t_dec, "value": E / t_dec, "unit": UNIT, "decompose_roofline": roof(2 * B_sup, t_dec),
+            "peak_gbs": peak,
+            "peel_mode": {2: "lists (one walk)", 1: "lists (two walks)"}.get(
+                res.listing, "search (24 T bytes of lists exceed the device budget)"),
             "ktruss": kt, "ktruss_equals_truss_ge_k": True}
+
+
+def _hbm_peak():
+    """(GB/s, 'measured' | 'fallback'): the copy bandwidth the pool measured on
+    this GPU model, else the fallback figure."""
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(peaks["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- reference GPU path
+def bench_reference_gpu(dev, g, ws, flow_scale=18, reps=3):
+    """The reference's own GPU kernels (myhpu_extension_kernel.cu compiled
+    unmodified for sm_103a; oracle/ref_gpu.py launches them as the
+    reference's launchers do) beside this build's, on the same GPU:
+
+    * support pass on the benchmark graph: checkElementsTwoPtrTile (K3,
+      kernel.cu:81-141, n_cut = 2) against the build's count walk
+      (tdt_triangle_count), CUDA events, same per-edge support required;
+    * the reference's `--cuda` flow (singlegpu_truss.py:67-158, restated in
+      flow.k_truss, its torch glue unchanged) over the reference's kernels
+      (K3, AllAffectedSupport_tilenot K7, segmentAdd K1) against
+      truss_decompose, on R-MAT(flow_scale), same e_truss / ptr_truss
+      required."""
+    import torch
+    try:
+        from oracle import ref_gpu as RG
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": "oracle/ref_gpu.py not importable: %s" % e}
+    if not RG.available():
+        return {"unavailable": "reference kernel image not built (oracle/build.py compiles it where the "
+                               "reference tree is present)"}
+    from tdtdecomposition_gb300 import CSRCOO, generators as G, truss as T
+    from tdtdecomposition_gb300.graph import tiling_row_ptr
+    from tdtdecomposition_gb300.preprocess import preprocess_edges
+    K = RG.RefKernels()
+    stream = torch.cuda.current_stream(dev)
+
+    def ev_time(fn, n):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(n):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    rows = g.rows if g.rows is not None else torch.repeat_interleave(
+        torch.arange(g.num_vertices, device=dev, dtype=torch.int32), g.row_ptr[1:] - g.row_ptr[:-1])
+    rpt = tiling_row_ptr(CSRCOO(columns=g.columns, row_ptr=g.row_ptr, rows=rows), 2)
+    out = torch.zeros(g.num_edges, dtype=torch.int32, device=dev)
+
+    def ref_support():
+        out.zero_()
+        K.segment_isin2tile(rows, g.columns, rpt, 2, out)
+
+    t_ref = ev_time(ref_support, reps)
+    _, sup = T.triangle_count(g, workspace=ws, return_support=True)
+    same = bool(torch.equal(out, sup))
+    t_ours = ev_time(lambda: T.triangle_count(g, workspace=ws), reps)
+    del out, rpt, sup
+    # the host-driven flow over the reference's kernels, R-MAT(flow_scale)
+    src, dst = G.rmat_edges_device(flow_scale, 16 << flow_scale, seed=1, device=dev)
+    h, verts = preprocess_edges(src, dst)
+    del src, dst
+    V, E = h.num_vertices, h.num_edges
+    wsf = T.Workspace(dev)
+    mine = T.truss_decompose(h, workspace=wsf)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mine = T.truss_decompose(h, workspace=wsf)
+    t_mine = time.perf_counter() - t0
+
+    def ref_flow():
+        gg = CSRCOO(columns=h.columns.clone(), row_ptr=tiling_row_ptr(h, 2), rows=h.rows.clone())
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res = RG.k_truss_on_reference_kernels(gg, 2, V, K)
+        torch.cuda.synchronize()
+        return res, time.perf_counter() - t
+
+    ref_flow()  # warm-up (module, allocator)
+    (kmax, et, pt), t_flow = ref_flow()
+    ident = (kmax == mine.kmax and torch.equal(et.to(dev), mine.e_truss)
+             and torch.equal(pt.cpu(), mine.ptr_truss.cpu()))
+    if not (same and ident):
+        print(json.dumps({"error": "reference GPU kernels disagree with the build", "support_equal": same,
+                          "flow_equal": ident}), file=sys.stderr, flush=True)
+    return {"image": "myhpu_extension_kernel.cu compiled unmodified for sm_103a",
+            "support_pass": {"workload": "the benchmark graph (E=%d), n_cut = 2" % g.num_edges,
+                             "reference_kernel": "checkElementsTwoPtrTile (K3)", "reference_ms": t_ref,
+                             "ours_kernel": "support_kernel (count walk, tdt_triangle_count)", "ours_ms": t_ours,
+                             "speedup": t_ref / t_ours, "same_support": same},
+            "flow": {"workload": "R-MAT scale %d, edge factor 16, seed 1 (V=%d, E=%d)" % (flow_scale, V, E),
+                     "reference": "singlegpu_truss.k_truss flow over the reference kernels (n_cut = 2)",
+                     "reference_s": t_flow, "reference_edges_per_s": E / t_flow,
+                     "ours": "truss_decompose", "ours_s": t_mine, "ours_edges_per_s": E / t_mine,
+                     "speedup": t_flow / t_mine, "results_identical": bool(ident)},
+            "reference_kernel_launches": K.launches}
+
+
+def bench_same_scale(dev, scale, reps):
+    """The GPU decomposition of exactly the graph the CPU arm times: R-MAT
+    (scale, 16 * 2^scale draws, seed 1), generated and preprocessed on the
+    device (the same edges and CSR as the oracle's).  Returns the line and
+    the per-edge truss numbers for the comparison with the CPU result."""
+    import torch
+    from tdtdecomposition_gb300 import generators as G, truss as T
+    from tdtdecomposition_gb300.preprocess import preprocess_edges
+    src, dst = G.rmat_edges_device(scale, 16 << scale, seed=1, device=dev)
+    g, _ = preprocess_edges(src, dst)
+    del src, dst
+    ws = T.Workspace(dev)
+    for _ in range(2):
+        T.truss_decompose(g, workspace=ws)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        res = T.truss_decompose(g, workspace=ws, sync=False)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    truss = res[0].cpu().numpy()
+    return {"scale": scale, "V": g.num_vertices, "E": g.num_edges, "gpu_ms": ms,
+            "gpu_value": g.num_edges / (ms / 1e3), "unit": UNIT}, truss
 
 
 # ---------------------------------------------------------------- fusion ablation
@@ -542,13 +701,15 @@ def bench_served_small(dev, srv, num_graphs=4096, rate=20000.0):
 
 
 # ---------------------------------------------------------------- GPU arm
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per decomposition
-# of R-MAT scale 22 / edge factor 16, per phase, from one ncu capture of
-# `bench.py --steps 1 --warmup 1 --no-cpu-baseline --no-batched --no-served`
-# (summarised in profiles/launches_rmat_s22_bench.md).
-MEASURED_TRAFFIC = {
-    (22, 16): {"support": 31.30e9, "listing": 150.5e9, "peel": 284.37e9, "outputs": 6.6e9, "setup": 2.4e9},
-}
+# DRAM bytes per triangle of each phase of a decomposition (the sum of
+# dram__bytes_read.sum + dram__bytes_write.sum over the phase's kernels), from
+# a one-pass ncu capture of the main launches of one R-MAT scale-20
+# decomposition (T = 423,980,669) of this build.  The lists, the staging area
+# and the peel's slots all grow with T, so a phase's traffic at another size
+# is its rate x T.  Reported beside the algorithmic bytes, never used for them.
+TRAFFIC_PER_TRIANGLE = {"support": 39.8, "listing": 66.1, "peel": 60.5}
+TRAFFIC_SOURCE = ("ncu one-pass capture (dram__bytes_read.sum + dram__bytes_write.sum) of one R-MAT scale-20 "
+                  "decomposition, scaled per triangle")
 
 
 def main_ours(args):
@@ -653,18 +814,12 @@ def main_ours(args):
 
     if rank != 0:
         return
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    peak, peak_src = _hbm_peak()
     n = max(nc.value, 1)
     t_sup, t_list, t_peel, t_post = (phases[k] / n for k in range(4))
     # the decomposition's algorithmic bytes B_dec = 2 B_sup: the support pass,
     # then one re-enumeration of each edge's triangles (listing + peel)
-    mt = MEASURED_TRAFFIC.get((scale, ef))
+    mt = {k: v * res.triangles for k, v in TRAFFIC_PER_TRIANGLE.items()}
     B_dec = 2 * B_sup
     ach = B_dec / (ms_step / 1e3) / 1e9
     phases_ms = {"support": t_sup, "listing": t_list, "peel": t_peel, "outputs": t_post}
@@ -683,7 +838,7 @@ def main_ours(args):
             "unit": "GB/s", "frac": ach / peak, "traffic": sum(mt.values()) if mt else None,
             "algorithmic_bytes": B_dec, "peak_source": peak_src, "per_kernel": per_kernel, "phase_ms": phases_ms,
             "peel_clock_ms": {k: round(v, 2) for k, v in peel_clk.items()},
-            "traffic_source": "ncu capture of this workload (profiles/launches_rmat_s22_bench.md)" if mt else None}
+            "traffic_source": TRAFFIC_SOURCE}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
@@ -703,18 +858,36 @@ def main_ours(args):
         line["batched"] = bench_batched(dev, args.steps, args.warmup)
     if not args.no_served:
         line["served"] = bench_served(dev)
-    if args.skewed:
+    # the benchmark's workspace (lists and staging, most of the device) goes
+    # before the other sections allocate theirs
+    wsp.buf = None
+    torch.cuda.empty_cache()
+    if not args.no_reference_gpu:
+        line["reference_gpu"] = bench_reference_gpu(dev, g, wsp)
+        wsp.buf = None
+        torch.cuda.empty_cache()
+    if not args.no_skewed:
         line["skewed"] = bench_skewed(dev, args.skewed_log2n)
+        torch.cuda.empty_cache()
     if args.fusion:
         line["fusion"] = bench_fusion(dev, args.fusion_scale)
     if args.undirected:
         line["undirected"] = bench_undirected(dev, args.fusion_scale)
+    sc = cpu_sample_scale(args, args.steps + args.warmup)
+    same, gpu_truss = (None, None) if args.no_same_scale else bench_same_scale(dev, sc, args.steps)
     if not args.no_cpu_baseline:
-        sc = cpu_sample_scale(args, 1)
-        Ec, Vc, times, threads = cpu_decompose_sample(sc, 1)
+        import numpy as np
+        Ec, Vc, times, threads, cpu_truss = cpu_decompose_sample(sc, 1)
         line["cpu_baseline"] = {"value": Ec / times[0], "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "R-MAT scale %d, 16*2^%d draws, seed 1 (V=%d, E=%d), one full "
                                           "decomposition, %.1f s" % (sc, sc, Vc, Ec, times[0])}
+        if same is not None:
+            same["cpu_value"] = Ec / times[0]
+            same["cpu_kind"] = "port (oracle restatement of the --cuda flow, OpenMP, %d threads)" % threads
+            same["gpu_over_cpu"] = same["gpu_value"] / same["cpu_value"]
+            same["results_identical"] = bool(np.array_equal(gpu_truss, cpu_truss))
+    if same is not None:
+        line["same_scale"] = same
     print(json.dumps(line), flush=True)
 
 
