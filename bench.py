@@ -599,43 +599,61 @@ def bench_undirected(dev, scale=18):
 
 
 # ---------------------------------------------------------------- served workload
-def bench_served(dev, n_requests=48, rates=(8.0, 32.0, 128.0, 512.0, 2048.0)):
-    """Poisson request streams (the same 48 seeded requests replayed at each
-    rate): half Barabasi-Albert (n log-uniform [256, 2^18], m in {4..16}),
-    half R-MAT (scale 12..20, edge factor 16); half full decompositions, half
-    k-truss searches (k uniform in [3, 20]); 150 GB admission budget."""
+def bench_served(dev, n_requests=1000, rates=(64.0, 256.0, 1024.0), n_resident=200):
+    """Poisson request streams (the same n_requests seeded requests replayed
+    at each rate): half Barabasi-Albert (n log-uniform [256, 2^18], m in
+    {4..16}), half R-MAT (scale 12..20, edge factor 16); half full
+    decompositions, half k-truss searches (k uniform in [3, 20]); 150 GB
+    admission budget.  The plain path serves the same requests one at a time
+    with the same per-request choice (copy in, preprocess, decompose -- or
+    the fixed-level search for a k-truss query on a graph of 2^19 edges or
+    more -- answer out).  Then n_resident follow-up queries (a k-truss at
+    another k, a decomposition, a triangle count) on graphs the last stream
+    kept resident, answered without ingest."""
+    import numpy as np
     import torch
     from tdtdecomposition_gb300 import serve as S, truss as T, workloads as W
     from tdtdecomposition_gb300.preprocess import preprocess_edges
     specs = W.request_stream(n_requests, rate_per_s=1.0, seed=7)
     base = S.make_requests(specs, device=dev)
     draws = sum(len(r.src) for r in base)
-    # plain: one request at a time (copy in, preprocess, decompose, answer out)
+    search_min = 1 << 19
     wsp, pps = T.Workspace(dev), T.Workspace(dev)
     big = max(base, key=lambda r: len(r.src))  # grows both workspaces before the timed loop
     gb, _ = preprocess_edges(big.src.to(dev), big.dst.to(dev), workspace=pps)
     T.truss_decompose(gb, workspace=wsp, list_budget=S.DEFAULT_LIST_BUDGET)
     del gb
-    s_plain = float("inf")
-    for _ in range(2):  # the faster of two passes (the plain time varies between passes)
-        plain_answers, edges = [], 0
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        for r in base:
-            g, _ = preprocess_edges(r.src.to(dev, non_blocking=True), r.dst.to(dev, non_blocking=True),
-                                    workspace=pps)
-            edges += g.num_edges
-            res = T.truss_decompose(g, workspace=wsp, list_budget=S.DEFAULT_LIST_BUDGET)
-            plain_answers.append(S.answer_for(r.query, res.truss).cpu())
-        s_plain = min(s_plain, time.perf_counter() - t1)
+    plain_answers, edges, sizes = [], 0, []
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for r in base:
+        g, _ = preprocess_edges(r.src.to(dev, non_blocking=True), r.dst.to(dev, non_blocking=True), workspace=pps)
+        edges += g.num_edges
+        sizes.append(g.num_edges)
+        if S.is_ktruss(r.query) and g.num_edges >= search_min:
+            a = T.ktruss_search(g, int(r.query[1]), workspace=wsp, lists=False)
+        else:
+            a = S.answer_for(r.query, T.truss_decompose(g, workspace=wsp, list_budget=S.DEFAULT_LIST_BUDGET).truss)
+        plain_answers.append(a.cpu())
+    s_plain = time.perf_counter() - t1
+    del wsp, pps
+    torch.cuda.empty_cache()
     out = {"workload": "Poisson stream of %d requests: half BA n log-uniform [256,2^18] m {4..16}, half R-MAT "
                        "scale 12..20 ef 16; half decompose, half k-truss k in [3,20]; 150 GB budget" % n_requests,
            "requests": n_requests, "edges": edges, "draws": draws,
-           "plain_value": edges / s_plain, "plain_s": s_plain, "rates": []}
-    srv = S.TrussServer(dev, memory_budget=150e9)
-    srv.run([S.Request(r.id, 0.0, r.src, r.dst, r.query) for r in base[:4]], real_time=False)  # warm-up
+           "requests_by_class": {name: int(sum(lo <= e < hi for e in sizes)) for name, lo, hi in S.SIZE_CLASSES},
+           "plain_value": edges / s_plain, "plain_s": s_plain,
+           "plain": "one request at a time: copy in, preprocess, decompose (or the fixed-level search for a "
+                    "k-truss query on >= 2^19 edges), answer out",
+           "server": {"max_batch_edges": 1 << 23, "max_wait_s": 0.25, "search_min_edges": search_min}, "rates": []}
+    srv = S.TrussServer(dev, memory_budget=150e9, search_min_edges=search_min)
+    srv.run([S.Request(r.id, 0.0, r.src, r.dst, r.query) for r in base[:8]], real_time=False)  # warm-up
+    reqs = None
     for lam in rates:
-        reqs = [S.Request(r.id, sp["arrival"] / lam, r.src, r.dst, r.query) for r, sp in zip(base, specs)]
+        keep_last = lam == rates[-1]
+        reqs = [S.Request(r.id, sp["arrival"] / lam, r.src, r.dst, r.query, handle=r.id,
+                          keep=keep_last and r.id % (n_requests // n_resident) == 0)
+                for r, sp in zip(base, specs)]
         srv.run(reqs, real_time=True)
         for r, a in zip(reqs, plain_answers):
             if not torch.equal(r.answer, a):
@@ -643,12 +661,33 @@ def bench_served(dev, n_requests=48, rates=(8.0, 32.0, 128.0, 512.0, 2048.0)):
         st = S.latency_stats(reqs)
         span = max(r.t_done for r in reqs) - min(r.arrival for r in reqs)
         out["rates"].append({"rate_per_s": lam, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-                             "value": edges / span, "unit": UNIT, "makespan_s": span})
+                             "value": edges / span, "unit": UNIT, "makespan_s": span,
+                             "by_class": S.latency_by_class(reqs),
+                             "paths": {p: sum(r.path == p for r in reqs) for p in ("batch", "search")}})
     best = max(out["rates"], key=lambda x: x["value"])
     out["value"] = best["value"]
     out["unit"] = UNIT
     out["speedup_vs_plain"] = best["value"] / out["plain_value"]
     out["results_identical_to_plain"] = True
+    # follow-up queries on the graphs the last stream kept resident
+    kept = [r for r in reqs if r.keep]
+    rng = np.random.default_rng(3)
+    follow = []
+    for i, r in enumerate(kept):
+        q = ("ktruss", int(rng.integers(3, 21))) if i % 3 == 0 else ("decompose" if i % 3 == 1 else "triangles")
+        follow.append(S.Request(n_requests + i, 0.0, None, None, q, handle=r.handle))
+    srv.run(follow, real_time=False)
+    checked = 0
+    for q, r in zip(follow, kept):
+        if q.query == "decompose":
+            ok = torch.equal(q.answer, plain_answers[r.id]) if r.query == "decompose" else True
+            checked += r.query == "decompose"
+            if not ok:
+                raise SystemExit("resident decomposition of request %d differs" % r.id)
+    st = S.latency_stats(follow)
+    out["resident_followups"] = {"queries": len(follow), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                                 "resident_graphs": len(srv.resident), "resident_bytes": srv.resident_bytes,
+                                 "decompositions_checked_against_plain": checked}
     out["small_graphs"] = bench_served_small(dev, srv)
     return out
 

@@ -1,7 +1,9 @@
 """Serving: continuous batching of decomposition and k-truss queries.
 
 A request carries a raw edge list on the host and a query (a full
-decomposition, or a k-truss search).  The server
+decomposition, a k-truss search, or -- on a resident graph -- a triangle
+count), or names a graph already resident on the server (a handle).  The
+server
 
 * admits arrived requests in arrival order while their estimated device
   footprint fits the memory budget (150 GB by default);
@@ -9,19 +11,30 @@ decomposition, or a k-truss search).  The server
   admitted since the last ingest as one group (one host-to-device copy, one
   grouped device preprocessing); their CSR then stays resident on the device
   until the request completes;
-* whenever the device is free, packs EVERY ingested request into one disjoint
-  union and decomposes it in one run (batch.decompose) — requests that arrive
-  while a batch runs join the next one, so work keeps flowing instead of
-  waiting for a full batch;
+* whenever the device is free, picks the next work: queries on resident
+  graphs first (answered from their cached truss numbers, or by one call on
+  the resident CSR); then a k-truss query on a large graph alone, by the
+  fixed-level peel of ktruss_search (ktruss_search/ktruss_cuda.py:383-463),
+  which touches only the low-support edges instead of decomposing the whole
+  graph; otherwise one disjoint union of the ingested requests, smallest
+  first (requests that have waited past max_wait_s go first), up to
+  max_batch_edges edges, decomposed in one run (batch.decompose) -- so small
+  requests do not wait behind a large graph's peel, and requests that arrive
+  while a batch runs join a later one;
 * answers each request from its slice of the union's truss numbers: the
   decomposition itself, or the k-truss as {e : truss(e) >= k} (exact: the
   k-truss is the set of edges whose truss number is at least k);
-* records latency = answer on the host - arrival.
+* keeps the graph of a request submitted with keep=True resident under its
+  handle (its CSR and truss numbers, least recently used evicted first past
+  resident_budget), so later queries on it need no ingest and, once decomposed,
+  no kernel at all;
+* records latency = answer on the host - arrival, and how each request was
+  answered (``path``: "batch", "search" or "resident").
 
-Only one decomposition runs at a time: its peel is a persistent cooperative
-kernel that needs every block resident, and two such kernels sharing the GPU
-could each wait for the other's blocks.  Overlap comes from ingest (copies and
-preprocessing on another stream) and result read-back running beside it.
+Only one peel runs at a time: it is a persistent cooperative kernel that needs
+every block resident, and two such kernels sharing the GPU could each wait for
+the other's blocks.  Overlap comes from ingest (copies and preprocessing on
+another stream) and result read-back running beside it.
 """
 import queue
 import threading
@@ -37,14 +50,17 @@ from .preprocess import group_offsets, preprocess_edges
 
 class Request:
     __slots__ = ("id", "arrival", "src", "dst", "query", "graph", "vertices", "answer", "t_done", "bytes",
-                 "num_edges", "t_admit", "t_ready")
+                 "num_edges", "t_admit", "t_ready", "handle", "keep", "path")
 
-    def __init__(self, rid, arrival, src, dst, query):
+    def __init__(self, rid, arrival, src, dst, query, handle=None, keep=False):
         self.id = rid
         self.arrival = arrival
-        self.src = src            # host int32 (pinned)
+        self.src = src            # host int32 (pinned); None for a query on a resident graph
         self.dst = dst
-        self.query = query        # "decompose" or ("ktruss", k)
+        self.query = query        # "decompose", ("ktruss", k) or, on a resident graph, "triangles"
+        self.handle = handle      # resident graph to query (src is None) or to keep this graph under
+        self.keep = bool(keep)
+        self.path = None          # how it was answered: "batch", "search" or "resident"
         self.graph = None
         self.vertices = None
         self.answer = None
@@ -52,7 +68,7 @@ class Request:
         self.t_admit = None
         self.t_ready = None
         self.num_edges = 0
-        self.bytes = footprint_bytes(len(src))
+        self.bytes = footprint_bytes(len(src)) if src is not None else 0
 
 
 def footprint_bytes(num_draws):
@@ -66,6 +82,21 @@ def answer_for(query, truss_slice):
     if query == "decompose":
         return truss_slice
     return truss_slice >= int(query[1])
+
+
+def is_ktruss(query):
+    return isinstance(query, tuple) and query[0] == "ktruss"
+
+
+class Resident:
+    """A graph kept on the device between queries: its CSR and, once known,
+    its truss numbers."""
+    __slots__ = ("graph", "truss", "bytes")
+
+    def __init__(self, graph, truss=None):
+        self.graph = graph
+        self.truss = truss
+        self.bytes = 16 * graph.num_edges + 8 * (graph.num_vertices + 1)
 
 
 # Workspace tail for triangle lists: the device keeps lists for a batch when
@@ -92,8 +123,18 @@ def take_group(inbox, max_draws):
 
 
 class TrussServer:
-    def __init__(self, device=None, memory_budget=150e9, max_batch_edges=1 << 28, list_budget=DEFAULT_LIST_BUDGET,
-                 max_group_draws=1 << 23):
+    """Continuous-batching server on one GPU.
+
+    memory_budget: device bytes the admitted requests may hold (estimated by
+    footprint_bytes); max_batch_edges: edges of one union (bounds the time a
+    union's peel holds the device, so the latency of the requests behind it);
+    max_wait_s: a request waiting longer goes into the next union first;
+    search_min_edges: k-truss queries on graphs with at least this many edges
+    run the fixed-level search alone; resident_budget: device bytes of the
+    graphs kept under handles (least recently used evicted first)."""
+
+    def __init__(self, device=None, memory_budget=150e9, max_batch_edges=1 << 23, list_budget=DEFAULT_LIST_BUDGET,
+                 max_group_draws=1 << 23, max_wait_s=0.25, search_min_edges=1 << 19, resident_budget=20e9):
         dev = torch.device(device) if device is not None else torch.device("cuda")
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
@@ -101,11 +142,16 @@ class TrussServer:
         self.budget = float(memory_budget)
         self.max_batch_edges = int(max_batch_edges)
         self.max_group_draws = int(max_group_draws)
+        self.max_wait_s = float(max_wait_s)
+        self.search_min_edges = int(search_min_edges)
+        self.resident_budget = float(resident_budget)
         self.list_budget = int(list_budget)  # workspace tail for triangle lists (device decides per batch)
         self.ingest_stream = torch.cuda.Stream(self.device)
         self.compute_stream = torch.cuda.Stream(self.device)
         self.ws = T.Workspace(self.device)
         self.pp_ws = T.Workspace(self.device)
+        self.resident = {}          # handle -> Resident, in least-recently-used order
+        self.resident_bytes = 0
 
     # ------------------------------------------------------------ ingest
     def _ingest_loop(self, inbox, ready):
@@ -161,7 +207,7 @@ class TrussServer:
         ingest = threading.Thread(target=self._ingest_loop, args=(inbox, ready), daemon=True)
         ingest.start()
         pending = list(requests)
-        waiting, resident = [], []
+        waiting, resident_q, chunks = [], [], []
         used = 0.0
         done = 0
         t0 = time.perf_counter()
@@ -173,7 +219,7 @@ class TrussServer:
                     r = pending.pop(0)
                     if not real_time:
                         r.arrival = now  # latency counted from submission
-                    waiting.append(r)
+                    (resident_q if r.src is None else waiting).append(r)
                 while waiting and used + waiting[0].bytes <= self.budget:
                     r = waiting.pop(0)
                     used += r.bytes
@@ -181,29 +227,30 @@ class TrussServer:
                     inbox.put(r)
                 while True:
                     try:
-                        resident.append(ready.get_nowait())
+                        chunks.append(ready.get_nowait())
                     except queue.Empty:
                         break
-                if not resident:
+                if resident_q:
+                    for r in resident_q:
+                        self._serve_resident(r)
+                    done += len(resident_q)
+                    resident_q = []
+                    continue
+                if not chunks:
                     if waiting and used == 0.0:
                         raise RuntimeError("request %d does not fit the memory budget" % waiting[0].id)
                     try:
-                        resident.append(ready.get(timeout=0.001))
+                        chunks.append(ready.get(timeout=0.001))
                     except queue.Empty:
                         if real_time and pending and not waiting:
                             time.sleep(max(0.0, min(0.002, pending[0].arrival - (time.perf_counter() - t0))))
                     continue
-                # one batch: every ingested chunk (up to max_batch_edges)
-                chunks, edges = [], 0
-                for ch in resident:
-                    e = ch[1].graph.num_edges
-                    if chunks and edges + e > self.max_batch_edges:
-                        break
-                    chunks.append(ch)
-                    edges += e
-                resident = resident[len(chunks):]
-                self._run_batch(chunks)
-                for reqs, _ in chunks:
+                work, chunks = self._pick(chunks, time.perf_counter() - t0)
+                if len(work) == 1 and len(work[0][0]) == 1 and self._searches(work[0][0][0]):
+                    self._run_search(work[0])
+                else:
+                    self._run_batch(work)
+                for reqs, _ in work:
                     for r in reqs:
                         used -= r.bytes
                     done += len(reqs)
@@ -211,6 +258,47 @@ class TrussServer:
             inbox.put(None)
             ingest.join(timeout=30)
         return requests
+
+    def _searches(self, r):
+        return is_ktruss(r.query) and r.num_edges >= self.search_min_edges
+
+    def _pick(self, chunks, now):
+        """The next work among the ingested chunks: a lone large k-truss query
+        (fixed-level search), else a union of chunks up to max_batch_edges
+        edges, those holding a request older than max_wait_s first, then the
+        smallest.  Returns (work, remaining chunks)."""
+        for i, ch in enumerate(chunks):
+            if len(ch[0]) == 1 and self._searches(ch[0][0]):
+                return [ch], chunks[:i] + chunks[i + 1:]
+
+        def key(ch):
+            oldest = min(r.arrival for r in ch[0])
+            return (0 if now - oldest > self.max_wait_s else 1, ch[1].graph.num_edges, oldest)
+
+        order = sorted(range(len(chunks)), key=lambda i: key(chunks[i]))
+        take, edges = [], 0
+        for i in order:
+            e = chunks[i][1].graph.num_edges
+            if take and edges + e > self.max_batch_edges:
+                continue
+            take.append(i)
+            edges += e
+        taken = set(take)
+        return [chunks[i] for i in sorted(take)], [c for i, c in enumerate(chunks) if i not in taken]
+
+    def _finish(self, reqs, outs, path):
+        self.compute_stream.synchronize()
+        t = time.perf_counter() - self.t0
+        for r, h in zip(reqs, outs):
+            r.answer = h
+            r.t_done = t
+            r.path = path
+
+    @staticmethod
+    def _to_host(a):
+        h = torch.empty(a.shape, dtype=a.dtype, pin_memory=True)
+        h.copy_(a, non_blocking=True)
+        return h
 
     def _run_batch(self, chunks):
         with torch.cuda.stream(self.compute_stream):
@@ -222,25 +310,77 @@ class TrussServer:
             else:
                 bt = pack_device([c[1].graph for c in chunks], self.device)
             res = B.decompose(bt, workspace=self.ws, list_budget=self.list_budget)
-            # per-request edge ranges inside the packed union
-            batch, eo = [], [0]
-            ebase = bt.edge_offsets.tolist()
+            # per-request vertex and edge ranges inside the packed union
+            batch, vr, er = [], [], []
+            ebase, vbase = bt.edge_offsets.tolist(), bt.vertex_offsets.tolist()
             for ci, (reqs, cb) in enumerate(chunks):
-                ceo = cb.edge_offsets.tolist()
+                ceo, cvo = cb.edge_offsets.tolist(), cb.vertex_offsets.tolist()
                 for i, r in enumerate(reqs):
                     batch.append(r)
-                    eo.append(ebase[ci] + ceo[i + 1])
+                    er.append((ebase[ci] + ceo[i], ebase[ci] + ceo[i + 1]))
+                    vr.append((vbase[ci] + cvo[i], vbase[ci] + cvo[i + 1]))
             outs = []
-            for i, r in enumerate(batch):
-                a = answer_for(r.query, res.truss[eo[i]:eo[i + 1]])
-                h = torch.empty(a.shape, dtype=a.dtype, pin_memory=True)
-                h.copy_(a, non_blocking=True)
-                outs.append(h)
-            self.compute_stream.synchronize()
-            t = time.perf_counter() - self.t0
-            for r, h in zip(batch, outs):
-                r.answer = h
-                r.t_done = t
+            for r, (a, b), (va, vb) in zip(batch, er, vr):
+                tr = res.truss[a:b]
+                outs.append(self._to_host(answer_for(r.query, tr)))
+                if r.keep:
+                    g = bt.graph
+                    sub = CSRCOO(columns=g.columns[a:b] - int(va), row_ptr=g.row_ptr[va:vb + 1] - int(a),
+                                 rows=g.rows[a:b] - int(va))
+                    self._keep(r.handle, sub, tr.clone())
+            self._finish(batch, outs, "batch")
+
+    def _run_search(self, chunk):
+        """One large k-truss query alone: the fixed-level peel on its graph."""
+        (r,), bt = chunk
+        with torch.cuda.stream(self.compute_stream):
+            for t in (bt.graph.columns, bt.graph.rows, bt.graph.row_ptr):
+                t.record_stream(self.compute_stream)
+            mask = T.ktruss_search(bt.graph, int(r.query[1]), workspace=self.ws, stream=self.compute_stream,
+                                   lists=False)
+            if r.keep:
+                self._keep(r.handle, bt.graph, None)
+            self._finish([r], [self._to_host(mask)], "search")
+
+    # ------------------------------------------------------------ resident graphs
+    def _keep(self, handle, graph, truss):
+        if handle is None:
+            raise ValueError("keep=True needs a handle")
+        old = self.resident.pop(handle, None)
+        if old is not None:
+            self.resident_bytes -= old.bytes
+        rs = Resident(graph, truss)
+        self.resident[handle] = rs
+        self.resident_bytes += rs.bytes
+        while self.resident_bytes > self.resident_budget and len(self.resident) > 1:
+            h = next(iter(self.resident))
+            self.resident_bytes -= self.resident.pop(h).bytes
+
+    def _serve_resident(self, r):
+        """A query on a resident graph: from its cached truss numbers when the
+        graph was decomposed, else one call on its resident CSR (the
+        decomposition's truss numbers are cached for the next query)."""
+        rs = self.resident.pop(r.handle, None)
+        if rs is None:
+            raise KeyError("graph %r is not resident on the server" % (r.handle,))
+        self.resident[r.handle] = rs  # most recently used
+        r.num_edges = rs.graph.num_edges
+        with torch.cuda.stream(self.compute_stream):
+            if r.query == "triangles":
+                a = torch.tensor([T.triangle_count(rs.graph, workspace=self.ws, stream=self.compute_stream)])
+            elif rs.truss is None and is_ktruss(r.query):
+                a = T.ktruss_search(rs.graph, int(r.query[1]), workspace=self.ws, stream=self.compute_stream,
+                                    lists=False)
+            else:
+                if rs.truss is None:
+                    rs.truss = T.truss_decompose(rs.graph, workspace=self.ws, stream=self.compute_stream,
+                                                 list_budget=self.list_budget).truss
+                a = answer_for(r.query, rs.truss)
+            self._finish([r], [self._to_host(a)], "resident")
+
+    def register(self, handle, graph):
+        """Keep an already preprocessed device graph resident under `handle`."""
+        self._keep(handle, graph, None)
 
 
 def pack_device(graphs, device):
@@ -277,3 +417,17 @@ def latency_stats(requests):
     lat = np.array([r.t_done - r.arrival for r in requests])
     return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "mean_ms": float(lat.mean() * 1e3)}
+
+
+SIZE_CLASSES = (("small (E < 2^16)", 0, 1 << 16), ("medium (2^16 <= E < 2^20)", 1 << 16, 1 << 20),
+                ("large (E >= 2^20)", 1 << 20, 1 << 62))
+
+
+def latency_by_class(requests):
+    """latency_stats per request-size class (edges after preprocessing)."""
+    out = {}
+    for name, lo, hi in SIZE_CLASSES:
+        rs = [r for r in requests if lo <= r.num_edges < hi]
+        if rs:
+            out[name] = dict(latency_stats(rs), requests=len(rs))
+    return out

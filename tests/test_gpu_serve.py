@@ -43,6 +43,61 @@ def test_each_result_same_alone_and_in_the_mix(budget):
     assert st["p99_ms"] >= st["p50_ms"] > 0
 
 
+def test_search_path_and_small_unions_give_the_same_answers():
+    """k-truss queries on graphs past search_min_edges run the fixed-level
+    search alone; the rest go into unions of at most max_batch_edges edges,
+    smallest first.  Every answer equals the request run alone."""
+    reqs = _requests(n=16, seed=5)
+    srv = S.TrussServer(search_min_edges=2000, max_batch_edges=30000, max_wait_s=0.0)
+    out = srv.run(reqs, real_time=False)
+    paths = {r.path for r in out}
+    assert "search" in paths and "batch" in paths
+    for r in out:
+        assert torch.equal(r.answer, _alone(r)), r.id
+        if r.path == "search":
+            assert S.is_ktruss(r.query) and r.num_edges >= 2000
+    by = S.latency_by_class(out)
+    assert sum(v["requests"] for v in by.values()) == len(out)
+
+
+def test_resident_graphs_answer_later_queries():
+    """Graphs kept under handles answer later queries without ingest: from
+    their cached truss numbers once decomposed (a batch kept them), or by one
+    call on the resident CSR (the search path kept them without truss
+    numbers); triangle counts on the resident CSR."""
+    reqs = _requests(n=8, seed=3)
+    for r in reqs:
+        r.keep, r.handle = True, "g%d" % r.id
+    srv = S.TrussServer(search_min_edges=2000)
+    srv.run(reqs, real_time=False)
+    assert set(srv.resident) == {r.handle for r in reqs}
+    later = []
+    for i, r in enumerate(reqs):
+        for q in ("decompose", ("ktruss", 3 + i % 4), "triangles"):
+            later.append(S.Request(100 + len(later), 0.0, None, None, q, handle=r.handle))
+    srv.run(later, real_time=False)
+    for q in later:
+        base = reqs[int(q.handle[1:])]
+        g, _ = preprocess_edges(base.src.cuda(), base.dst.cuda())
+        assert q.path == "resident"
+        if q.query == "triangles":
+            assert int(q.answer[0]) == T.triangle_count(g)
+        else:
+            assert torch.equal(q.answer, S.answer_for(q.query, T.truss_decompose(g, lists=False).truss).cpu())
+
+
+def test_resident_budget_evicts_least_recently_used():
+    reqs = _requests(n=6, seed=9)
+    for r in reqs:
+        r.keep, r.handle = True, r.id
+    srv = S.TrussServer(resident_budget=1)  # keeps only the most recent graph
+    srv.run(reqs, real_time=False)
+    assert len(srv.resident) == 1
+    gone = next(r.handle for r in reqs if r.handle not in srv.resident)
+    with pytest.raises(KeyError):
+        srv.run([S.Request(99, 0.0, None, None, "decompose", handle=gone)], real_time=False)
+
+
 def test_pack_device_is_the_disjoint_union():
     from tdtdecomposition_gb300 import batch as B
     gs = []
