@@ -1270,7 +1270,7 @@ int test_barrier_timeout(void* ws, long long limit_ns, cudaStream_t st) {
 }
 
 int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* cA, int32_t* cB,
-                         int32_t* cC, void* ctl, const int* gate, cudaStream_t st);
+                         int32_t* cC, void* ctl, const int* gate, int* status, cudaStream_t st);
 int launch_support_list(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, const int64_t* off,
                         const int32_t* cA, const int32_t* cB, unsigned long long* curA_g,
                         unsigned long long* curB_g, int2* lists, void* ctl, const int* gate, int* status,
@@ -1406,7 +1406,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     if (mode == 2) {
         // triangle count: the count-only walk (skipped on the device when
         // validation failed)
-        rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->g.status, st);
+        rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->g.status, &L.ctl->g.status, st);
         if (rc) return rc;
         init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
         TDT_LAUNCH_CHECK("init_state");
@@ -1451,7 +1451,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     rc = launch_support_stage(rp, cols, V, E, L.soff, L.bnd, cA, cB, cC, curA, curB, stage_end, stage_slots,
                               L.sup_ctl, &L.ctl->stage_skip, &L.ctl->g.status, st);
     if (rc) return rc;
-    rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->roles_skip, st);
+    rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->roles_skip, &L.ctl->g.status, st);
     if (rc) return rc;
     init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
     TDT_LAUNCH_CHECK("init_state");

@@ -437,6 +437,95 @@ __device__ __forceinline__ RowState stage_row(const OutRows<Off>& G, const SupAr
     return R;
 }
 
+// ---- heavy rows staged by one bulk copy (TMA, cp.async.bulk) ----------------
+// A heavy row's middle part (the 16-byte aligned span of cols[bu, bu+d)) is
+// copied into shared memory by one bulk copy that thread 0 issues and an
+// mbarrier tracks; meanwhile the block clears the bitmap and counters and
+// loads the ragged ends with plain loads.  The row buffer starts (bu mod 4)
+// entries into its area so that su[i] and cols[bu + i] share their address
+// mod 16 (the copy needs 16-byte aligned source and destination and a size in
+// whole 16 bytes).  The wait is bounded: past kBulkWaitNs the block records
+// TDT_ERR_TIMEOUT (the run's result is then rejected) and goes on.
+#ifndef TDT_BULK_STAGE
+#define TDT_BULK_STAGE 1
+#endif
+constexpr uint64_t kBulkWaitNs = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Thread 0: order the block's earlier accesses of the buffer (made visible to
+// it by the preceding __syncthreads) before the async proxy's writes, then
+// expect `bytes` on the barrier and start the copy.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return done != 0;
+}
+
+// Thread 0: wait for the copy of phase `phase` (bounded); true when it landed.
+__device__ __noinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase) {
+    const uint64_t t0 = globaltimer_ns();
+    for (unsigned it = 1;; it++) {
+        if (mbar_try_wait(bar, phase)) return true;
+        if ((it & 63u) == 0 && globaltimer_ns() - t0 > kBulkWaitNs) return false;
+    }
+}
+
+// Stage heavy row u (d entries at bu, d + 3 <= kHeavyCap) by a bulk copy;
+// the same RowState as stage_row's in-shared-memory case.  Called by the
+// whole block right after a __syncthreads.
+template <int M, class Off>
+__device__ __forceinline__ RowState stage_row_bulk(const OutRows<Off>& G, const SupArgs& A, int32_t* su_area,
+                                                   uint32_t* cnt_buf, uint32_t* bm, int bm_log2, Off bu, int d,
+                                                   uint64_t* bar, unsigned& phase) {
+    RowState R;
+    int32_t* su = su_area + (int)(bu & 3);
+    const Off a0 = (bu + 3) & ~(Off)3, a1 = (bu + d) & ~(Off)3;
+    const bool bulk = a1 > a0;
+    if (threadIdx.x == 0 && bulk) bulk_copy_g2s(su + (a0 - bu), G.cols + a0, 4u * (unsigned)(a1 - a0), bar);
+    for (int i = threadIdx.x; i < (1 << bm_log2) / 32; i += kSupBlock) bm[i] = 0u;
+    for (int i = threadIdx.x; i < d; i += kSupBlock) {
+        cnt_buf[i] = 0u;
+        if (!bulk || i < (int)(a0 - bu) || i >= (int)(a1 - bu)) su[i] = __ldg(G.cols + bu + i);
+    }
+    if (threadIdx.x == 0 && bulk) {
+        if (!mbar_wait_bounded(bar, phase) && A.status) atomicMax(A.status, (int)TDT_ERR_TIMEOUT);
+        phase ^= 1u;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < d; i += kSupBlock) {
+        const uint32_t h = bm_hash(su[i], bm_log2);
+        atomicOr(bm + (h >> 5), 1u << (h & 31));
+    }
+    R.bu = bu;
+    R.d = d;
+    R.bm = bm;
+    R.bm_log2 = bm_log2;
+    R.packed = true;
+    R.su = su;
+    R.cnt = cnt_buf;
+    R.umax = d > 0 ? __ldg(G.cols + bu + d - 1) : INT32_MIN;
+    return R;
+}
+
 template <int M>
 __device__ __forceinline__ void flush_row(const RowState& R, const SupArgs& A, int tid, int nthr) {
     const int d = R.d;
@@ -505,6 +594,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
     __shared__ int32_t s_wsum[2][kSupWarps + 1];
     __shared__ int s_n;
     __shared__ long long s_chunk;
+    __shared__ __align__(8) uint64_t s_bar;  // bulk copies of heavy rows
     const int wib = threadIdx.x / kWarp;
     const unsigned lane = lane_id();
     const int64_t nv = G.nv;
@@ -515,6 +605,11 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
 
     // ---- phase 1: rows with d+(u) > warp_cap, one block per row
     {
+        // bulk staging needs 16-byte aligned columns (kVec) and a status word
+        // for a wait that runs out
+        const bool bulk_ok = TDT_BULK_STAGE && kVec && A.status != nullptr;
+        unsigned phase = 0;
+        if (threadIdx.x == 0 && bulk_ok) mbar_init(&s_bar, 1);  // first used after the next __syncthreads
         int32_t* h_su = reinterpret_cast<int32_t*>(smem);
         uint32_t* h_cnt = reinterpret_cast<uint32_t*>(smem + 4 * kHeavyCap);
         int32_t* g_S = reinterpret_cast<int32_t*>(smem + kHvS);
@@ -546,8 +641,10 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                 const int d = (int)(G.end(u) - bu);
                 const bool in_smem = d <= heavy_cap;
                 uint32_t* bm = in_smem ? reinterpret_cast<uint32_t*>(smem + kHvBm) : reinterpret_cast<uint32_t*>(smem);
-                RowState R = stage_row<M>(G, A, h_su, h_cnt, bm, in_smem ? kHeavyBmLog2 : kHugeBmLog2, in_smem, bu, d,
-                                          threadIdx.x, kSupBlock, true);
+                RowState R = (bulk_ok && in_smem && d + 3 <= kHeavyCap)
+                                 ? stage_row_bulk<M>(G, A, h_su, h_cnt, bm, kHeavyBmLog2, bu, d, &s_bar, phase)
+                                 : stage_row<M>(G, A, h_su, h_cnt, bm, in_smem ? kHeavyBmLog2 : kHugeBmLog2, in_smem,
+                                                bu, d, threadIdx.x, kSupBlock, true);
                 __syncthreads();
                 const int vend = kIdOrdered ? d - 1 : d;
                 for (int g0 = 0; g0 < vend; g0 += kSeg) {
@@ -737,7 +834,7 @@ int launch_support_accum_i32(const int32_t* rp, int32_t stride, const int32_t* c
 // atomics for rows searched in place), cC accumulated by atomics: the caller
 // zeroes all three first.
 int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int64_t ne, int32_t* cA, int32_t* cB,
-                         int32_t* cC, void* ctl, const int* gate, cudaStream_t st) {
+                         int32_t* cC, void* ctl, const int* gate, int* status, cudaStream_t st) {
     if (nv <= 0) return TDT_OK;
     OutRows<int64_t> G{rp, 1, cols, nv, ne};
     SupArgs A{};
@@ -745,6 +842,7 @@ int launch_support_roles(const int64_t* rp, const int32_t* cols, int64_t nv, int
     A.cB = cB;
     A.cC = cC;
     A.gate = gate;
+    A.status = status;
     return launch_mode<kSupRoles, true, int64_t>(G, A, reinterpret_cast<SupCtl*>(ctl), st);
 }
 

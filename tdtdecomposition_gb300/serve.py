@@ -104,16 +104,23 @@ class Resident:
 DEFAULT_LIST_BUDGET = 24e9
 
 
-def take_group(inbox, max_draws):
+def take_group(inbox, max_draws, alone=None, carry=None):
     """The next ingest group: block for one request, then take what is
     already queued while the group holds fewer than max_draws edge draws.
-    None in the queue ends the stream.  Returns (group, stop)."""
-    group = [inbox.get()]
+    None in the queue ends the stream.  A request for which alone(r) holds
+    forms a group of its own: met inside a group, it is kept in `carry` (a
+    list) and starts the next one.  Returns (group, stop)."""
+    group = [carry.pop(0) if carry else inbox.get()]
+    if group[0] is not None and alone is not None and alone(group[0]):
+        return group, False
     draws = len(group[0].src) if group[0] is not None else 0
     while group[-1] is not None and draws < max_draws:
         try:
             r = inbox.get_nowait()
         except queue.Empty:
+            break
+        if r is not None and alone is not None and alone(r):
+            carry.append(r)
             break
         group.append(r)
         if r is not None:
@@ -161,14 +168,21 @@ class TrussServer:
         shifted per request, ranks grouped per request), so a group of small
         requests costs one set of launches.  The cap lets the decomposition of
         a first group start while a burst of arrivals is still being
-        ingested."""
+        ingested.  Large k-truss queries are ingested alone (the search
+        path)."""
         torch.cuda.set_device(self.device)
+        carry = []
         with torch.cuda.stream(self.ingest_stream):
             stop = False
             while not stop:
-                group, stop = take_group(inbox, self.max_group_draws)
+                group, stop = take_group(inbox, self.max_group_draws, self._search_candidate, carry)
                 if group:
                     ready.put(self._ingest_group(group))
+
+    def _search_candidate(self, r):
+        """A k-truss query whose edge list may reach search_min_edges edges
+        after preprocessing: ingested alone, so it can take the search path."""
+        return is_ktruss(r.query) and len(r.src) >= self.search_min_edges
 
     def _ingest_group(self, group):
         nids = []

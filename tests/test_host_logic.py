@@ -101,3 +101,26 @@ def test_server_ingest_groups_are_capped():
 
     q.put(None)
     assert S.take_group(q, 8) == ([], True)
+
+
+def test_server_ingests_search_candidates_alone():
+    """A request the server may answer by the fixed-level search (a k-truss
+    query on a large edge list) forms an ingest group of its own; one met in
+    the middle of a group is carried to the next."""
+    import queue
+    from tdtdecomposition_gb300 import serve as S
+
+    def req(i, n, q="decompose"):
+        return S.Request(i, 0.0, torch.zeros(n, dtype=torch.int32), torch.zeros(n, dtype=torch.int32), q)
+
+    alone = lambda r: S.is_ktruss(r.query) and len(r.src) >= 5  # noqa: E731
+    q, carry = queue.Queue(), []
+    for r in (req(0, 2), req(1, 6, ("ktruss", 4)), req(2, 2), req(3, 2, ("ktruss", 3)), req(4, 9, ("ktruss", 5))):
+        q.put(r)
+    q.put(None)
+    groups = []
+    stop = False
+    while not stop:
+        g, stop = S.take_group(q, 100, alone, carry)
+        groups.append([r.id for r in g])
+    assert groups == [[0], [1], [2, 3], [4], []]
