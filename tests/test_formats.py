@@ -14,8 +14,11 @@ from tdtdecomposition_gb300 import formats as F
 from tdtdecomposition_gb300.graph import CSRCOO
 from tests import _golden as GD
 
-# the reference tree, where present: its loader and its binary-CSR tool pin the formats
-REF = os.environ.get("TDT_REFERENCE_ROOT", "/root/reference")
+# golden files written by the reference's own converter and CSRCOO class
+# (tests/golden/make_format_golden.py); the reference tree itself is used only
+# when TDT_REFERENCE_ROOT names it
+REF = os.environ.get("TDT_REFERENCE_ROOT")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def _write_text(path, pairs, header=True):
@@ -72,7 +75,17 @@ def test_pth_loader_refuses_other_classes(tmp_path):
         F.load_pth(p)
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree absent")
+def test_pth_written_by_the_reference_class_loads_here():
+    """A file torch.save wrote from the reference's own CSRCOO class (int32
+    row_ptr, as read_prepro_save writes it) loads as the same graph."""
+    g = _graph()
+    h = F.load_pth(os.path.join(GOLDEN, "fmt_ref_csrcoo.pth"))
+    assert torch.equal(h.columns, g.columns) and torch.equal(h.rows, g.rows)
+    assert torch.equal(h.row_ptr.to(torch.int64), g.row_ptr)
+
+
+@pytest.mark.skipif(REF is None or not os.path.isdir(os.path.join(REF, "src")),
+                    reason="TDT_REFERENCE_ROOT does not name the reference tree")
 def test_pth_interoperates_with_the_reference_class(tmp_path):
     """Our reference-compatible file loads as the reference's own CSRCOO, and a
     file the reference's class wrote loads here."""
@@ -109,10 +122,20 @@ def test_binary_csr_round_trip(tmp_path):
     assert set(zip(a.tolist(), b.tolist())) == want and len(a) == len(want)
 
 
-@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "demo_truss/test/txt_to_csrcoo.cpp"))
-                    or shutil.which("g++") is None, reason="reference tool or g++ absent")
 def test_binary_csr_matches_reference_tool(tmp_path):
-    """write_csr_bin produces the same bytes as the reference's converter."""
+    """write_csr_bin produces the same bytes as the reference's converter
+    (txt_to_csrcoo.cpp) wrote for the same edge list."""
+    pairs = np.load(os.path.join(GOLDEN, "fmt_csr_pairs.npy"))
+    F.write_csr_bin(str(tmp_path / "ours"), pairs[:, 0], pairs[:, 1])
+    for name in ("csr_vlist.bin", "csr_elist.bin"):
+        with open(os.path.join(GOLDEN, "fmt_csr_ref", name), "rb") as f:
+            assert (tmp_path / "ours" / name).read_bytes() == f.read(), name
+
+
+@pytest.mark.skipif(REF is None or not os.path.isfile(os.path.join(str(REF), "demo_truss/test/txt_to_csrcoo.cpp"))
+                    or shutil.which("g++") is None, reason="TDT_REFERENCE_ROOT does not name the reference tree")
+def test_binary_csr_matches_reference_tool_live(tmp_path):
+    """The same against the reference's converter built and run here."""
     rng = np.random.default_rng(5)
     pairs = rng.integers(0, 300, size=(2000, 2)) * 3 + 1
     txt = tmp_path / "g.txt"
