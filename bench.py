@@ -747,9 +747,18 @@ def bench_served_small(dev, srv, num_graphs=4096, rate=20000.0):
 # decomposition (T = 423,980,669) of this build.  The lists, the staging area
 # and the peel's slots all grow with T, so a phase's traffic at another size
 # is its rate x T.  Reported beside the algorithmic bytes, never used for them.
-TRAFFIC_PER_TRIANGLE = {"support": 39.8, "listing": 66.1, "peel": 60.5}
+TRAFFIC_PER_TRIANGLE = {"support": 41.2, "listing": 66.4, "peel": 60.5}
 TRAFFIC_SOURCE = ("ncu one-pass capture (dram__bytes_read.sum + dram__bytes_write.sum) of one R-MAT scale-20 "
                   "decomposition, scaled per triangle")
+# The same DRAM bytes per decomposition of R-MAT scale 22, edge factor 16,
+# from one-kernel, one-launch, one-pass captures of the main kernels at that
+# size (the one walk 130.8 GB, compaction 83.3 GB, transpose 56.2 GB, peel
+# 154.5 GB; the in-adjacency and bounds kernels scaled from scale 20): at
+# this size the peel's edge states no longer fit in L2, so its rate per
+# triangle is higher than at scale 20.
+TRAFFIC_BY_WORKLOAD = {(22, 16): {"support": 133.1e9, "listing": 139.5e9, "peel": 154.5e9}}
+TRAFFIC_SOURCE_BY_WORKLOAD = ("ncu one-kernel, one-launch, one-pass captures (dram__bytes_read.sum + "
+                              "dram__bytes_write.sum) of the main kernels of one decomposition of this workload")
 
 
 def main_ours(args):
@@ -859,7 +868,8 @@ def main_ours(args):
     t_sup, t_list, t_peel, t_post = (phases[k] / n for k in range(4))
     # the decomposition's algorithmic bytes B_dec = 2 B_sup: the support pass,
     # then one re-enumeration of each edge's triangles (listing + peel)
-    mt = {k: v * res.triangles for k, v in TRAFFIC_PER_TRIANGLE.items()}
+    mt = TRAFFIC_BY_WORKLOAD.get((scale, ef)) or {k: v * res.triangles for k, v in TRAFFIC_PER_TRIANGLE.items()}
+    traffic_src = TRAFFIC_SOURCE_BY_WORKLOAD if (scale, ef) in TRAFFIC_BY_WORKLOAD else TRAFFIC_SOURCE
     B_dec = 2 * B_sup
     ach = B_dec / (ms_step / 1e3) / 1e9
     phases_ms = {"support": t_sup, "listing": t_list, "peel": t_peel, "outputs": t_post}
@@ -878,7 +888,7 @@ def main_ours(args):
             "unit": "GB/s", "frac": ach / peak, "traffic": sum(mt.values()) if mt else None,
             "algorithmic_bytes": B_dec, "peak_source": peak_src, "per_kernel": per_kernel, "phase_ms": phases_ms,
             "peel_clock_ms": {k: round(v, 2) for k, v in peel_clk.items()},
-            "traffic_source": TRAFFIC_SOURCE}
+            "traffic_source": traffic_src}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",

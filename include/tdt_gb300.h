@@ -85,6 +85,14 @@ void tdt_set_support_caps(int warp_cap, int heavy_cap);
  * calls launched afterwards from any thread. */
 void tdt_set_vector_walk(int on);
 
+/* Knob of the support/listing kernels: 1 stages the rows that a whole block
+ * walks (out-degree above 256) into shared memory by one bulk copy
+ * (cp.async.bulk, tracked by an mbarrier with a bounded wait) plus plain
+ * loads of the ragged ends; 0 (the default) loads them with plain loads.
+ * Needs the vectorised walk.  Results do not depend on it.  Affects calls
+ * launched afterwards from any thread. */
+void tdt_set_bulk_staging(int on);
+
 /* Testing knobs of the failure paths (no counterpart in the reference, which
  * has no bounded waits).  tdt_set_peel_deadline_ns: wall-clock budget of the
  * peel launches that follow (<= 0 restores the default of 120 s); a run past

@@ -121,6 +121,7 @@ struct SupArgs {
     unsigned long long stage_cap;   // kSupStage: slots the staging area holds; no store at or past it
     const int* gate;                // non-zero: skip the pass
     int* status;                    // kSupList: set when a row's slots do not end where counted
+    int bulk;                       // stage heavy rows by a bulk copy (needs kVec and a status word)
     int warp_cap;                   // rows with d+ <= warp_cap go to one warp (<= kWarpCap)
     int heavy_cap;                  // heavier rows staged in smem up to this size (<= kHeavyCap)
 };
@@ -131,6 +132,9 @@ static int g_warp_cap = 0, g_heavy_cap = 0;
 // Test hook: 0 forces the scalar wedge walk (the vectorised one is the default).
 static int g_vec_walk = 1;
 void set_vector_walk(int on) { g_vec_walk = on != 0; }
+// Heavy rows staged by a bulk copy (1) or plain loads (0, the default).
+static int g_bulk_stage = 0;
+void set_bulk_staging(int on) { g_bulk_stage = on != 0; }
 void set_support_caps(int warp_cap, int heavy_cap) {
     g_warp_cap = warp_cap;
     g_heavy_cap = heavy_cap;
@@ -446,9 +450,10 @@ __device__ __forceinline__ RowState stage_row(const OutRows<Off>& G, const SupAr
 // mod 16 (the copy needs 16-byte aligned source and destination and a size in
 // whole 16 bytes).  The wait is bounded: past kBulkWaitNs the block records
 // TDT_ERR_TIMEOUT (the run's result is then rejected) and goes on.
-#ifndef TDT_BULK_STAGE
-#define TDT_BULK_STAGE 1
-#endif
+// Off by default (tdt_set_bulk_staging): at R-MAT scale 22 the support phase
+// took 65.1 ms with it against 63.7 ms with plain loads (the copy has to land
+// before the bitmap is built, where plain loads overlap the two), a tie at
+// scale 20.
 constexpr uint64_t kBulkWaitNs = 2000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -607,7 +612,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
     {
         // bulk staging needs 16-byte aligned columns (kVec) and a status word
         // for a wait that runs out
-        const bool bulk_ok = TDT_BULK_STAGE && kVec && A.status != nullptr;
+        const bool bulk_ok = kVec && A.bulk && A.status != nullptr;
         unsigned phase = 0;
         if (threadIdx.x == 0 && bulk_ok) mbar_init(&s_bar, 1);  // first used after the next __syncthreads
         int32_t* h_su = reinterpret_cast<int32_t*>(smem);
@@ -805,6 +810,7 @@ static int launch_mode(const OutRows<Off>& G, const SupArgs& A, SupCtl* ctl, cud
     SupArgs A2 = A;
     A2.warp_cap = (g_warp_cap > 0 && g_warp_cap < kWarpCap) ? g_warp_cap : kWarpCap;
     A2.heavy_cap = (g_heavy_cap > 0 && g_heavy_cap < kHeavyCap) ? g_heavy_cap : kHeavyCap;
+    A2.bulk = g_bulk_stage;
     // the vectorised walk needs 16-byte aligned columns (chunk positions stay
     // below 2^31 under 2^30 edges)
     const bool vec = g_vec_walk && ((uintptr_t)G.cols & 15u) == 0 && G.ne < (1ll << 30);

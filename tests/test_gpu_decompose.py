@@ -160,12 +160,13 @@ def test_repeatable_and_workspace_reuse():
     assert torch.equal(a.truss, b.truss) and torch.equal(a.e_truss, b.e_truss)
 
 
-@pytest.mark.parametrize("vec", [1, 0])
+@pytest.mark.parametrize("vec,bulk", [(1, 0), (1, 1), (0, 0)])
 @pytest.mark.parametrize("caps", [(4, 16), (8, 10 ** 6), (2, 3)])
-def test_all_support_paths_vs_oracle(caps, vec):
+def test_all_support_paths_vs_oracle(caps, vec, bulk):
     """Lowered light/heavy thresholds push small graphs through the block-level
     heavy-row walk and the in-place (beyond shared memory) path, with the
-    wedge walk over 16-byte column chunks and over single columns."""
+    wedge walk over 16-byte column chunks and over single columns, and the
+    heavy rows staged by plain loads or by a bulk copy."""
     from tdtdecomposition_gb300 import _lib
     L = _lib.load()
     s, d = G.rmat_edges(12, 16 << 12, seed=31)
@@ -174,6 +175,7 @@ def test_all_support_paths_vs_oracle(caps, vec):
     sup_ref = O.support(rows, cols, rp.astype(np.int32), 1)
     L.tdt_set_support_caps(*caps)
     L.tdt_set_vector_walk(vec)
+    L.tdt_set_bulk_staging(bulk)
     try:
         t, sup = T.triangle_count(graph_of(rows, cols, rp), return_support=True)
         assert np.array_equal(sup.cpu().numpy(), sup_ref)
@@ -187,6 +189,7 @@ def test_all_support_paths_vs_oracle(caps, vec):
     finally:
         L.tdt_set_support_caps(0, 0)
         L.tdt_set_vector_walk(1)
+        L.tdt_set_bulk_staging(0)
 
 
 def test_unaligned_columns_take_the_scalar_walk():
