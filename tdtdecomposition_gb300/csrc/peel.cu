@@ -620,6 +620,8 @@ struct Window {
     long long base_l;   // first slot of that item
     long long i0n;      // item of slot cb+32
     long long base0n;   // its first slot
+    long long nsn;      // first slot of item i0n + 1 (-1: not among the loaded starts)
+    bool starts_next;   // item i0n starts at cb+32 (no lane of this window holds it)
 };
 
 __device__ __forceinline__ Window locate(const long long* __restrict__ qb, long long N, long long i0,
@@ -635,14 +637,56 @@ __device__ __forceinline__ Window locate(const long long* __restrict__ qb, long 
     const int nb = __popc(mk);
     const long long Bn = __shfl_sync(kFull, B, nb);
     const long long Bl = __shfl_sync(kFull, B, (nb + 31) & 31);
-    if (Bn == cb + kWarp) {
+    const long long B2 = __shfl_sync(kFull, B, (nb + 1) & 31);
+    w.starts_next = Bn == cb + kWarp;
+    if (w.starts_next) {
         w.i0n = i0 + nb + 1;
         w.base0n = Bn;
+        w.nsn = nb + 1 < kWarp ? B2 : -1;
     } else {
         w.i0n = i0 + nb;
         w.base0n = nb > 0 ? Bl : base0;
+        w.nsn = nb < kWarp ? Bn : -1;
     }
     return w;
+}
+
+// The items of one window [cb, cb + 32) of a warp's range: this lane's item
+// record and first slot.  The warp keeps its current item i0 (holding slot
+// cb, or ending just before it when item i0 + 1 starts at cb; locate handles
+// both), that item's first slot, the first slot of the next item (nst, -1 when
+// unknown) and the item's record (rec, valid when rv): a window that lies
+// wholly in item i0 -- most windows, since most slots belong to long lists --
+// needs no load at all; otherwise one locate step and one record load per
+// lane, which also refresh the state.
+__device__ __forceinline__ void window_items(const long long* __restrict__ qb, const int4* __restrict__ qi,
+                                             long long N, long long cb, bool valid, unsigned le, long long& i0,
+                                             long long& base0, long long& nst, int4& rec, bool& rv, int4& it,
+                                             long long& base_l) {
+    if (nst >= cb + kWarp) {
+        if (!rv) {
+            rec = __ldcg(qi + i0);
+            rv = true;
+        }
+        it = rec;
+        base_l = base0;
+        return;
+    }
+    const Window w = locate(qb, N, i0, base0, cb, le);
+    it = make_int4(0, 0, 0, 0);
+    if (valid) it = __ldcg(qi + i0 + w.k);
+    base_l = w.base_l;
+    // lane 31 holds item i0n unless that item starts at cb + 32 (or lane 31
+    // lies past the range)
+    const bool v31 = (__ballot_sync(kFull, valid) >> 31) != 0u;
+    rec.x = __shfl_sync(kFull, it.x, 31);
+    rec.y = __shfl_sync(kFull, it.y, 31);
+    rec.z = __shfl_sync(kFull, it.z, 31);
+    rec.w = __shfl_sync(kFull, it.w, 31);
+    rv = v31 && !w.starts_next;
+    i0 = w.i0n;
+    base0 = w.base0n;
+    nst = w.nsn;
 }
 
 // The other two edges (f, g) of slot tl of item it; false when the slot is
@@ -741,21 +785,22 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         i0 = lo;
     }
     long long base0 = __ldcg(qb + i0);
+    long long nst = i0 + 1 < N ? __ldcg(qb + i0 + 1) : LLONG_MAX;
+    int4 rec = __ldcg(qi + i0);
+    bool rv = true;
     for (long long cb = cb0; cb < cb1; cb += 2 * kWarp) {
-        const Window wa = locate(qb, N, i0, base0, cb, le);
         const long long cb2 = cb + kWarp;
         const bool has_b = cb2 < cb1;
-        Window wb;
-        if (has_b) wb = locate(qb, N, wa.i0n, wa.base0n, cb2, le);
         const long long ta = cb + lane, tb = cb2 + lane;
         const bool va = ta < cb1, vb = has_b && tb < cb1;
-        int4 ita = make_int4(0, 0, 0, 0), itb = make_int4(0, 0, 0, 0);
-        if (va) ita = __ldcg(qi + i0 + wa.k);
-        if (vb) itb = __ldcg(qi + wa.i0n + wb.k);
+        int4 ita, itb = make_int4(0, 0, 0, 0);
+        long long bla, blb = 0;
+        window_items(qb, qi, N, cb, va, le, i0, base0, nst, rec, rv, ita, bla);
+        if (has_b) window_items(qb, qi, N, cb2, vb, le, i0, base0, nst, rec, rv, itb, blb);
         int32_t fa = 0, ga = 0, fb = 0, gb = 0;
         bool tra = false, trb = false;
-        if (va) tra = slot_edges<Listed>(A, ita, ta - wa.base_l, fa, ga);
-        if (vb) trb = slot_edges<Listed>(A, itb, tb - wb.base_l, fb, gb);
+        if (va) tra = slot_edges<Listed>(A, ita, ta - bla, fa, ga);
+        if (vb) trb = slot_edges<Listed>(A, itb, tb - blb, fb, gb);
         // dead-bit filter: a triangle with an edge peeled before round r is gone
         if (kDeadFilter) {
             unsigned xa = 0, ya = 0, xb = 0, yb = 0;
@@ -814,13 +859,6 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         } else {
             warp_append2_direct<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, &A.ctl->fe[nslot]);
             warp_append2_direct<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, &A.ctl->fe[nslot]);
-        }
-        if (has_b) {
-            i0 = wb.i0n;
-            base0 = wb.base0n;
-        } else {
-            i0 = wa.i0n;
-            base0 = wa.base0n;
         }
     }
     if (!dyn) break;
