@@ -361,6 +361,13 @@ constexpr bool kSkipMarked = TDT_SKIP_MARKED != 0;
 #endif
 constexpr bool kDeadFilter = TDT_DEAD_FILTER != 0;
 
+// The decrement results of a peel step are used one step later, after the
+// next step's loads are in flight (0: used at once).
+#ifndef TDT_PEEL_DEFER
+#define TDT_PEEL_DEFER 1
+#endif
+constexpr bool kPeelDefer = TDT_PEEL_DEFER != 0;
+
 #ifndef TDT_PEEL_STEP
 #define TDT_PEEL_STEP 8
 #endif
@@ -718,6 +725,34 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
     return gg >= 0;
 }
 
+// The decrements of one peel step: the four edges and the supports before
+// their decrements (INT32_MIN: no decrement).  An edge whose support fell to
+// l is marked for sub-round r+1 and queued; a larger result lowers the bound
+// dm of the next level.
+struct Pending {
+    int32_t e[4];
+    int32_t o[4];
+};
+
+template <bool Listed>
+__device__ __forceinline__ void settle(const PeelArgs& A, const Pending& P, int r, int32_t l, int nslot, int nbuf,
+                                       AppendBuf& B, int32_t& dm) {
+    bool w[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        w[j] = P.o[j] == l + 1;
+        if (P.o[j] > l + 1) dm = P.o[j] - 1 < dm ? P.o[j] - 1 : dm;
+        if (w[j]) A.es[P.e[j]].y = r + 1;
+    }
+    if (Listed) {
+        warp_append2_staged<Listed>(A, nslot, nbuf, w[0], P.e[0], w[1], P.e[1], l, B, &A.ctl->fe[nslot]);
+        warp_append2_staged<Listed>(A, nslot, nbuf, w[2], P.e[2], w[3], P.e[3], l, B, &A.ctl->fe[nslot]);
+    } else {
+        warp_append2_direct<Listed>(A, nslot, nbuf, w[0], P.e[0], w[1], P.e[1], l, &A.ctl->fe[nslot]);
+        warp_append2_direct<Listed>(A, nslot, nbuf, w[2], P.e[2], w[3], P.e[3], l, &A.ctl->fe[nslot]);
+    }
+}
+
 // One sub-round: warps gwarp = 0..nwarps-1 share the candidate slots of round r.
 // The smallest decrement result above l is folded into *dmin (the lower bound
 // of the next level).  Each step covers two 32-slot windows whose loads and
@@ -760,6 +795,12 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     long long cb0 = gwarp * per_warp;
     long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
     if (!dyn && cb0 >= cb1) return;
+    Pending P;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        P.e[j] = 0;
+        P.o[j] = INT32_MIN;
+    }
     for (;;) {
     if (dyn) {
         unsigned long long c = 0;
@@ -824,6 +865,8 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
             rfb = __ldcg(&A.es[fb].y);
             rgb = __ldcg(&A.es[gb].y);
         }
+        // the previous step's decrement results, while these loads are in flight
+        if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
         // a triangle is alive when both other edges are alive or peel in r or r+1;
         // which of f, g this lane decrements: the ownership rules above
         bool dfa = false, dga = false, dfb = false, dgb = false;
@@ -837,32 +880,24 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
             dfb = !ff && (!fg || itb.x < gb) && (!kSkipMarked || rfb != r + 1);
             dgb = !fg && (!ff || itb.x < fb) && (!kSkipMarked || rgb != r + 1);
         }
-        // issue all decrements before using any result
-        int32_t ofa = 0, oga = 0, ofb = 0, ogb = 0;
-        if (dfa) ofa = atomicSub(&A.es[fa].x, 1);
-        if (dga) oga = atomicSub(&A.es[ga].x, 1);
-        if (dfb) ofb = atomicSub(&A.es[fb].x, 1);
-        if (dgb) ogb = atomicSub(&A.es[gb].x, 1);
-        const bool wfa = dfa && ofa == l + 1, wga = dga && oga == l + 1;
-        const bool wfb = dfb && ofb == l + 1, wgb = dgb && ogb == l + 1;
-        if (dfa && ofa > l + 1) dm = ofa - 1 < dm ? ofa - 1 : dm;
-        if (dga && oga > l + 1) dm = oga - 1 < dm ? oga - 1 : dm;
-        if (dfb && ofb > l + 1) dm = ofb - 1 < dm ? ofb - 1 : dm;
-        if (dgb && ogb > l + 1) dm = ogb - 1 < dm ? ogb - 1 : dm;
-        if (wfa) A.es[fa].y = r + 1;
-        if (wga) A.es[ga].y = r + 1;
-        if (wfb) A.es[fb].y = r + 1;
-        if (wgb) A.es[gb].y = r + 1;
-        if (Listed) {
-            warp_append2_staged<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, B, &A.ctl->fe[nslot]);
-            warp_append2_staged<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, B, &A.ctl->fe[nslot]);
-        } else {
-            warp_append2_direct<Listed>(A, nslot, nbuf, wfa, fa, wga, ga, l, &A.ctl->fe[nslot]);
-            warp_append2_direct<Listed>(A, nslot, nbuf, wfb, fb, wgb, gb, l, &A.ctl->fe[nslot]);
+        // issue all decrements; their results are used by the next step
+        P.e[0] = fa;
+        P.e[1] = ga;
+        P.e[2] = fb;
+        P.e[3] = gb;
+        P.o[0] = dfa ? atomicSub(&A.es[fa].x, 1) : INT32_MIN;
+        P.o[1] = dga ? atomicSub(&A.es[ga].x, 1) : INT32_MIN;
+        P.o[2] = dfb ? atomicSub(&A.es[fb].x, 1) : INT32_MIN;
+        P.o[3] = dgb ? atomicSub(&A.es[gb].x, 1) : INT32_MIN;
+        if (!kPeelDefer) {
+            settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
+#pragma unroll
+            for (int j = 0; j < 4; j++) P.o[j] = INT32_MIN;
         }
     }
     if (!dyn) break;
     }
+    if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
     if (Listed) append_flush<Listed>(A, nslot, nbuf, B, &A.ctl->fe[nslot]);
     fold_min(dmin, dm);
 }
