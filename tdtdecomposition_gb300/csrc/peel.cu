@@ -90,6 +90,9 @@ struct PeelArgs {
     // filter in L2 that keeps most dead triangles away from the edge states;
     // a bit not set yet only costs the state check it would have saved)
     unsigned* dead;
+    // round code of edge e in the 4 bits at (e & 7) * 4 of word e >> 3 (the
+    // listed peel's partner-state check; see code_round)
+    unsigned* code;
     const int64_t* off;   // listed mode: list offsets int64[E+1]
     const int2* lists;    // listed mode: partner edge pairs
     int64_t V, E, round_cap;
@@ -108,6 +111,32 @@ __device__ __forceinline__ void set_status(PeelCtl* c, int s) {
 
 __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long* p) {
     return __ldcg(p);
+}
+
+// Round codes: 4 bits per edge, 32 MB at 64 M edges, so they stay in L2.
+// 0xF: never marked (alive); 0-3: marked for sub-round y, stored as y & 3;
+// bit 3 set: peeled and done.  A code is set once, when its edge is marked
+// (0xF -> y & 3, one atomicAnd), and turned dead during sub-round y + 1 with
+// the dead bits of that round's items (atomicOr 0x8).  An edge marked without
+// an item (no triangle left to enumerate) is dead at once: each of its
+// triangles is already destroyed by a partner peeled before it.  Hence, in
+// sub-round r (a grid barrier after every sub-round), a code reads 0xF
+// alive, r & 3 peeling in r, (r + 1) & 3 marked for r + 1, and anything else
+// peeled before r (an edge of r - 1 may still carry (r + 3) & 3).
+constexpr unsigned kCodeAlive = 0xFu, kCodeDead = 0x8u;
+
+__device__ __forceinline__ void code_mark(unsigned* code, int32_t e, unsigned c) {
+    atomicAnd(code + (e >> 3), ~((kCodeAlive ^ c) << ((unsigned)(e & 7) * 4u)));
+}
+
+// The sub-round stamp of edge e read from its code word in sub-round r: -1
+// alive, r or r + 1, or -2 for peeled before r.
+__device__ __forceinline__ int32_t code_round(unsigned word, int32_t e, int r) {
+    const unsigned c = (word >> ((unsigned)(e & 7) * 4u)) & 15u;
+    if (c == kCodeAlive) return -1;
+    if (c == ((unsigned)r & 3u)) return r;
+    if (c == ((unsigned)(r + 1) & 3u)) return r + 1;
+    return -2;
 }
 
 // Queue item of edge e (listed: e's list offset and length; search: the
@@ -368,6 +397,13 @@ constexpr bool kDeadFilter = TDT_DEAD_FILTER != 0;
 #endif
 constexpr bool kPeelDefer = TDT_PEEL_DEFER != 0;
 
+// The listed peel reads its partners' round codes instead of the dead bits
+// and the edge states (0: dead bits, then edge states).
+#ifndef TDT_PEEL_CODES
+#define TDT_PEEL_CODES 1
+#endif
+constexpr bool kPeelCodes = TDT_PEEL_CODES != 0;
+
 #ifndef TDT_PEEL_STEP
 #define TDT_PEEL_STEP 8
 #endif
@@ -479,7 +515,10 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
                 ok += __popc(km[u]);
                 os += __popc(wm[u]);
                 const bool want = keep[u] && sv[u] == g;
-                if (want) A.es[e[u]].y = r_next;
+                if (want) {
+                    A.es[e[u]].y = r_next;
+                    code_mark(A.code, e[u], sv[u] > 0 ? ((unsigned)r_next & 3u) : kCodeDead);
+                }
                 warp_append_staged(A, listed, slot, buf, want, e[u], sv[u], B, &A.ctl->pfe[np % 3]);
             }
             __syncthreads();  // s_tk / s_base are reused by the next tile
@@ -514,7 +553,10 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
             }
             const bool want = i < ns && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
-            if (want) A.es[e].y = r_next;
+            if (want) {
+                A.es[e].y = r_next;
+                code_mark(A.code, e, sv > 0 ? ((unsigned)r_next & 3u) : kCodeDead);
+            }
             warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
         }
     } else {
@@ -529,7 +571,10 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
             }
             const bool want = i < n2 && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
-            if (want) A.es[e].y = r_next;
+            if (want) {
+                A.es[e].y = r_next;
+                code_mark(A.code, e, sv > 0 ? ((unsigned)r_next & 3u) : kCodeDead);
+            }
             warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
         }
     }
@@ -584,7 +629,10 @@ __device__ __forceinline__ void warp_append_capped(const PeelArgs& A, bool liste
     old = __shfl_sync(kFull, old, 0);
     // edges without candidates use no queue space and are always taken
     const bool acc = want && (!q || ok);
-    if (acc) A.es[e].y = r_next;
+    if (acc) {
+        A.es[e].y = r_next;
+        code_mark(A.code, e, q ? ((unsigned)r_next & 3u) : kCodeDead);
+    }
     const unsigned ma = __ballot_sync(kFull, acc);
     if (lane == 0 && ma) atomicAdd(nfront, (unsigned long long)__popc(ma));
     if (q && ok) {
@@ -738,11 +786,17 @@ template <bool Listed>
 __device__ __forceinline__ void settle(const PeelArgs& A, const Pending& P, int r, int32_t l, int nslot, int nbuf,
                                        AppendBuf& B, int32_t& dm) {
     bool w[4];
+    // queued with an item when the level is above 0 (an edge without
+    // triangles never appears in a list, so its code is never read)
+    const unsigned cm = l > 0 ? ((unsigned)(r + 1) & 3u) : kCodeDead;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         w[j] = P.o[j] == l + 1;
         if (P.o[j] > l + 1) dm = P.o[j] - 1 < dm ? P.o[j] - 1 : dm;
-        if (w[j]) A.es[P.e[j]].y = r + 1;
+        if (w[j]) {
+            A.es[P.e[j]].y = r + 1;
+            code_mark(A.code, P.e[j], cm);
+        }
     }
     if (Listed) {
         warp_append2_staged<Listed>(A, nslot, nbuf, w[0], P.e[0], w[1], P.e[1], l, B, &A.ctl->fe[nslot]);
@@ -784,6 +838,7 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         for (long long i = gwarp * kWarp + lane; i < nprev; i += nwarps * kWarp) {
             const int32_t e = __ldcg(&qp[i].x);
             atomicOr(A.dead + (e >> 5), 1u << (e & 31));
+            atomicOr(A.code + (e >> 3), kCodeDead << ((unsigned)(e & 7) * 4u));
         }
     }
     // listed mode: each warp owns a contiguous range of candidate slots (a
@@ -842,31 +897,54 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         bool tra = false, trb = false;
         if (va) tra = slot_edges<Listed>(A, ita, ta - bla, fa, ga);
         if (vb) trb = slot_edges<Listed>(A, itb, tb - blb, fb, gb);
-        // dead-bit filter: a triangle with an edge peeled before round r is gone
-        if (kDeadFilter) {
+        int32_t rfa = -2, rga = -2, rfb = -2, rgb = -2;
+        if (Listed && kPeelCodes) {
+            // the partners' round codes (L2): dead, alive, peeling now, marked
             unsigned xa = 0, ya = 0, xb = 0, yb = 0;
             if (tra) {
-                xa = A.dead[fa >> 5];
-                ya = A.dead[ga >> 5];
+                xa = __ldcg(A.code + (fa >> 3));
+                ya = __ldcg(A.code + (ga >> 3));
             }
             if (trb) {
-                xb = A.dead[fb >> 5];
-                yb = A.dead[gb >> 5];
+                xb = __ldcg(A.code + (fb >> 3));
+                yb = __ldcg(A.code + (gb >> 3));
             }
-            if (tra && (((xa >> (fa & 31)) | (ya >> (ga & 31))) & 1u)) tra = false;
-            if (trb && (((xb >> (fb & 31)) | (yb >> (gb & 31))) & 1u)) trb = false;
+            // the previous step's decrement results, while these loads are in flight
+            if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
+            if (tra) {
+                rfa = code_round(xa, fa, r);
+                rga = code_round(ya, ga, r);
+            }
+            if (trb) {
+                rfb = code_round(xb, fb, r);
+                rgb = code_round(yb, gb, r);
+            }
+        } else {
+            // dead-bit filter: a triangle with an edge peeled before round r is gone
+            if (kDeadFilter) {
+                unsigned xa = 0, ya = 0, xb = 0, yb = 0;
+                if (tra) {
+                    xa = A.dead[fa >> 5];
+                    ya = A.dead[ga >> 5];
+                }
+                if (trb) {
+                    xb = A.dead[fb >> 5];
+                    yb = A.dead[gb >> 5];
+                }
+                if (tra && (((xa >> (fa & 31)) | (ya >> (ga & 31))) & 1u)) tra = false;
+                if (trb && (((xb >> (fb & 31)) | (yb >> (gb & 31))) & 1u)) trb = false;
+            }
+            if (tra) {
+                rfa = __ldcg(&A.es[fa].y);
+                rga = __ldcg(&A.es[ga].y);
+            }
+            if (trb) {
+                rfb = __ldcg(&A.es[fb].y);
+                rgb = __ldcg(&A.es[gb].y);
+            }
+            // the previous step's decrement results, while these loads are in flight
+            if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
         }
-        int32_t rfa = -2, rga = -2, rfb = -2, rgb = -2;
-        if (tra) {
-            rfa = __ldcg(&A.es[fa].y);
-            rga = __ldcg(&A.es[ga].y);
-        }
-        if (trb) {
-            rfb = __ldcg(&A.es[fb].y);
-            rgb = __ldcg(&A.es[gb].y);
-        }
-        // the previous step's decrement results, while these loads are in flight
-        if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
         // a triangle is alive when both other edges are alive or peel in r or r+1;
         // which of f, g this lane decrements: the ownership rules above
         bool dfa = false, dga = false, dfb = false, dgb = false;
@@ -1388,6 +1466,7 @@ struct Layout {
     int32_t* bnd;
     int32_t* alive[2];
     unsigned* dead;
+    unsigned* code;
     void* scan_ws;
     void* sort_ws;
     size_t total;
@@ -1417,6 +1496,7 @@ Layout carve(void* ws, int64_t V, int64_t E) {
     L.alive[0] = (int32_t*)c.take(4 * e);
     L.alive[1] = (int32_t*)c.take(4 * e);
     L.dead = (unsigned*)c.take(4 * (e / 32 + 1));
+    L.code = (unsigned*)c.take(4 * (e / 8 + 1));
     size_t scan_b = scan_scratch_bytes((int64_t)(e > v ? e : v) + 1);
     L.scan_ws = c.take(scan_b);
     L.sort_ws = c.take(radix_sort_scratch_bytes((int64_t)e));
@@ -1566,6 +1646,8 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     }
     A.dead = L.dead;
     TDT_CUDA(cudaMemsetAsync(L.dead, 0, 4 * (size_t)(E / 32 + 1), st));
+    A.code = L.code;
+    TDT_CUDA(cudaMemsetAsync(L.code, 0xff, 4 * (size_t)(E / 8 + 1), st));
     A.off = L.off; A.lists = lists;
     A.alive[0] = L.alive[0]; A.alive[1] = L.alive[1];
     A.V = V; A.E = E; A.round_cap = E + 2;
