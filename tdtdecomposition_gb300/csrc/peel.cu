@@ -79,7 +79,8 @@ struct PeelArgs {
     const int64_t* cp;
     const int32_t* in_src;
     const int32_t* in_eid;
-    int2* es;             // edge state {support, round}: round -1 = alive, else the sub-round that peeled it
+    int32_t* live;        // support of each edge, decremented as its triangles are destroyed
+    int32_t* rnd;         // sub-round that peeled each edge (-1: alive)
     int32_t* round_level;
     // queue of round r in buffer r % 3: round r reads r, appends r+1, and the
     // items of round r-1 stay intact for the dead bits set during round r
@@ -473,9 +474,11 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
                 keep[u] = false;
                 sv[u] = 0;
                 if (i < ncur) {
-                    const int2 st = __ldcg(A.es + e[u]);
-                    keep[u] = st.y == -1;
-                    sv[u] = st.x;
+                    // alive = never marked (its round code, in L2); the
+                    // support is a 4-byte gather
+                    const unsigned cw = __ldcg(A.code + (e[u] >> 3));
+                    sv[u] = __ldcg(A.live + e[u]);
+                    keep[u] = ((cw >> ((unsigned)(e[u] & 7) * 4u)) & 15u) == kCodeAlive;
                 }
             }
             unsigned km[kStep], wm[kStep];
@@ -516,7 +519,7 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
                 os += __popc(wm[u]);
                 const bool want = keep[u] && sv[u] == g;
                 if (want) {
-                    A.es[e[u]].y = r_next;
+                    A.rnd[e[u]] = r_next;
                     code_mark(A.code, e[u], sv[u] > 0 ? ((unsigned)r_next & 3u) : kCodeDead);
                 }
                 warp_append_staged(A, listed, slot, buf, want, e[u], sv[u], B, &A.ctl->pfe[np % 3]);
@@ -554,7 +557,7 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
             const bool want = i < ns && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
             if (want) {
-                A.es[e].y = r_next;
+                A.rnd[e] = r_next;
                 code_mark(A.code, e, sv > 0 ? ((unsigned)r_next & 3u) : kCodeDead);
             }
             warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
@@ -567,12 +570,12 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
             int32_t e = 0, sv = INT32_MAX;
             if (i < n2) {
                 e = __ldcg(nxt + i);
-                sv = __ldcg(&A.es[e].x);
+                sv = __ldcg(A.live + e);
             }
             const bool want = i < n2 && sv == m;
             if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
             if (want) {
-                A.es[e].y = r_next;
+                A.rnd[e] = r_next;
                 code_mark(A.code, e, sv > 0 ? ((unsigned)r_next & 3u) : kCodeDead);
             }
             warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
@@ -630,7 +633,7 @@ __device__ __forceinline__ void warp_append_capped(const PeelArgs& A, bool liste
     // edges without candidates use no queue space and are always taken
     const bool acc = want && (!q || ok);
     if (acc) {
-        A.es[e].y = r_next;
+        A.rnd[e] = r_next;
         code_mark(A.code, e, q ? ((unsigned)r_next & 3u) : kCodeDead);
     }
     const unsigned ma = __ballot_sync(kFull, acc);
@@ -656,9 +659,9 @@ __device__ bool fixed_collect(const PeelArgs& A, bool listed, int32_t l, int r_n
         bool want = false;
         int32_t s = 0;
         if (e < A.E) {
-            const int2 st = __ldcg(A.es + e);
-            s = st.x;
-            want = st.y == -1 && s <= l;
+            const unsigned cw = __ldcg(A.code + (e >> 3));
+            s = __ldcg(A.live + e);
+            want = ((cw >> ((unsigned)(e & 7) * 4u)) & 15u) == kCodeAlive && s <= l;
         }
         warp_append_capped(A, listed, slot, buf, want, (int32_t)e, s, r_next, &A.ctl->pfe[np % 3]);
     }
@@ -794,7 +797,7 @@ __device__ __forceinline__ void settle(const PeelArgs& A, const Pending& P, int 
         w[j] = P.o[j] == l + 1;
         if (P.o[j] > l + 1) dm = P.o[j] - 1 < dm ? P.o[j] - 1 : dm;
         if (w[j]) {
-            A.es[P.e[j]].y = r + 1;
+            A.rnd[P.e[j]] = r + 1;
             code_mark(A.code, P.e[j], cm);
         }
     }
@@ -898,7 +901,7 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         if (va) tra = slot_edges<Listed>(A, ita, ta - bla, fa, ga);
         if (vb) trb = slot_edges<Listed>(A, itb, tb - blb, fb, gb);
         int32_t rfa = -2, rga = -2, rfb = -2, rgb = -2;
-        if (Listed && kPeelCodes) {
+        if (kPeelCodes) {
             // the partners' round codes (L2): dead, alive, peeling now, marked
             unsigned xa = 0, ya = 0, xb = 0, yb = 0;
             if (tra) {
@@ -935,12 +938,12 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
                 if (trb && (((xb >> (fb & 31)) | (yb >> (gb & 31))) & 1u)) trb = false;
             }
             if (tra) {
-                rfa = __ldcg(&A.es[fa].y);
-                rga = __ldcg(&A.es[ga].y);
+                rfa = __ldcg(A.rnd + fa);
+                rga = __ldcg(A.rnd + ga);
             }
             if (trb) {
-                rfb = __ldcg(&A.es[fb].y);
-                rgb = __ldcg(&A.es[gb].y);
+                rfb = __ldcg(A.rnd + fb);
+                rgb = __ldcg(A.rnd + gb);
             }
             // the previous step's decrement results, while these loads are in flight
             if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
@@ -963,10 +966,10 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
         P.e[1] = ga;
         P.e[2] = fb;
         P.e[3] = gb;
-        P.o[0] = dfa ? atomicSub(&A.es[fa].x, 1) : INT32_MIN;
-        P.o[1] = dga ? atomicSub(&A.es[ga].x, 1) : INT32_MIN;
-        P.o[2] = dfb ? atomicSub(&A.es[fb].x, 1) : INT32_MIN;
-        P.o[3] = dgb ? atomicSub(&A.es[gb].x, 1) : INT32_MIN;
+        P.o[0] = dfa ? atomicSub(A.live + fa, 1) : INT32_MIN;
+        P.o[1] = dga ? atomicSub(A.live + ga, 1) : INT32_MIN;
+        P.o[2] = dfb ? atomicSub(A.live + fb, 1) : INT32_MIN;
+        P.o[3] = dgb ? atomicSub(A.live + gb, 1) : INT32_MIN;
         if (!kPeelDefer) {
             settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
 #pragma unroll
@@ -1118,7 +1121,8 @@ __global__ void csc_fill_kernel(const int32_t* __restrict__ rows, const int32_t*
 // {sup, alive}, triangle total.
 __global__ void init_state_kernel(const int32_t* __restrict__ cA, const int32_t* __restrict__ cB,
                                   const int32_t* __restrict__ cC, int32_t* __restrict__ sup,
-                                  int2* __restrict__ es, int64_t E, PeelCtl* ctl) {
+                                  int32_t* __restrict__ live, int32_t* __restrict__ rnd, int64_t E,
+                                  PeelCtl* ctl) {
     __shared__ long long s_part[32];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int i = 0; i < 3; i++) ctl->mgt[i] = INT32_MAX;
@@ -1130,7 +1134,8 @@ __global__ void init_state_kernel(const int32_t* __restrict__ cA, const int32_t*
          e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t s = cA[e] + cB[e] + cC[e];
         sup[e] = s;
-        es[e] = make_int2(s, -1);
+        live[e] = s;
+        rnd[e] = -1;
         acc += s;
     }
     acc = warp_sum(acc);
@@ -1282,13 +1287,13 @@ __global__ void list_cursor_kernel(const int64_t* __restrict__ off, const int32_
     }
 }
 
-__global__ void truss_out_kernel(const int2* __restrict__ es, const int32_t* __restrict__ round_level,
+__global__ void truss_out_kernel(const int32_t* __restrict__ rnd, const int32_t* __restrict__ round_level,
                                  int64_t E, int32_t* __restrict__ truss, uint32_t* __restrict__ keys,
                                  uint32_t* __restrict__ vals, PeelCtl* ctl) {
     if (ctl->g.status != 0) return;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t r = es[e].y;
+        const int32_t r = rnd[e];
         if (r < 0) {  // every edge is peeled when the run completes
             atomicMax((int*)&ctl->g.status, (int)TDT_ERR_CAPACITY);
             continue;
@@ -1340,13 +1345,13 @@ __global__ void ptr_etruss_kernel(const uint32_t* __restrict__ keys, const uint3
     }
 }
 
-__global__ void ktruss_out_kernel(const int2* __restrict__ es, int64_t E, uint8_t* __restrict__ in_k,
+__global__ void ktruss_out_kernel(const int32_t* __restrict__ rnd, int64_t E, uint8_t* __restrict__ in_k,
                                   PeelCtl* ctl) {
     __shared__ unsigned long long s_part[32];
     unsigned long long acc = 0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const uint8_t a = es[e].y == -1;
+        const uint8_t a = rnd[e] == -1;
         in_k[e] = a;
         acc += a;
     }
@@ -1457,7 +1462,8 @@ struct Layout {
     int32_t* in_src;
     int32_t* in_eid;
     int32_t* sup;
-    int2* es;
+    int32_t* live;
+    int32_t* rnd;
     int32_t* round_level;
     int4* qi[3];
     long long* qb[3];
@@ -1484,7 +1490,8 @@ Layout carve(void* ws, int64_t V, int64_t E) {
     L.in_src = (int32_t*)c.take(4 * e);
     L.in_eid = (int32_t*)c.take(4 * e);
     L.sup = (int32_t*)c.take(4 * e);
-    L.es = (int2*)c.take(8 * e);
+    L.live = (int32_t*)c.take(4 * e);
+    L.rnd = (int32_t*)c.take(4 * e);
     L.round_level = (int32_t*)c.take(4 * (e + 2));
     for (int b = 0; b < 3; b++) {
         L.qi[b] = (int4*)c.take(16 * e);
@@ -1561,7 +1568,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
         // validation failed)
         rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->g.status, &L.ctl->g.status, st);
         if (rc) return rc;
-        init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
+        init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.live, L.rnd, E, L.ctl);
         TDT_LAUNCH_CHECK("init_state");
         prof_mark(1, st);
         if (support_out) TDT_CUDA(cudaMemcpyAsync(support_out, L.sup, 4 * (size_t)E, cudaMemcpyDeviceToDevice, st));
@@ -1606,7 +1613,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     if (rc) return rc;
     rc = launch_support_roles(rp, cols, V, E, cA, cB, cC, L.sup_ctl, &L.ctl->roles_skip, &L.ctl->g.status, st);
     if (rc) return rc;
-    init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.es, E, L.ctl);
+    init_state_kernel<<<g_e, tb, 0, st>>>(cA, cB, cC, L.sup, L.live, L.rnd, E, L.ctl);
     TDT_LAUNCH_CHECK("init_state");
     prof_mark(1, st);
     // per-edge triangle lists in the workspace tail when 24 T bytes fit
@@ -1639,7 +1646,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     }
     PeelArgs A;
     A.rp = rp; A.cols = cols; A.rows = rows_use; A.cp = L.cp; A.in_src = L.in_src; A.in_eid = L.in_eid;
-    A.es = L.es; A.round_level = L.round_level;
+    A.live = L.live; A.rnd = L.rnd; A.round_level = L.round_level;
     for (int b = 0; b < 3; b++) {
         A.qi[b] = L.qi[b];
         A.qb[b] = L.qb[b];
@@ -1683,7 +1690,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
         uint32_t* vals = keys + E;
         uint32_t* keys_alt = reinterpret_cast<uint32_t*>(L.qi[1]);
         uint32_t* vals_alt = keys_alt + E;
-        truss_out_kernel<<<g_e, tb, 0, st>>>(L.es, L.round_level, E, truss, keys, vals, L.ctl);
+        truss_out_kernel<<<g_e, tb, 0, st>>>(L.rnd, L.round_level, E, truss, keys, vals, L.ctl);
         TDT_LAUNCH_CHECK("truss_out");
         const uint32_t* sk = keys;
         const uint32_t* sv = vals;
@@ -1699,7 +1706,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
         stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 0);
         TDT_LAUNCH_CHECK("stats_final");
     } else {
-        ktruss_out_kernel<<<g_e, tb, 0, st>>>(L.es, E, in_k, L.ctl);
+        ktruss_out_kernel<<<g_e, tb, 0, st>>>(L.rnd, E, in_k, L.ctl);
         TDT_LAUNCH_CHECK("ktruss_out");
         stats_final_kernel<<<1, 1, 0, st>>>(L.ctl, stats, 1);
         TDT_LAUNCH_CHECK("stats_final");
