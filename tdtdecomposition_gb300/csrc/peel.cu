@@ -51,7 +51,6 @@ struct PeelCtl {
     unsigned long long q[4];      // packed (items << kCandBits | candidates) per round slot
     unsigned long long fe[4];     // frontier edges per round slot (queued or not)
     unsigned long long cnt[3];     // survivors written by level change t, at t % 3
-    unsigned long long side_n[3];  // side-list length of level-change pass k, at k % 3
     unsigned long long pfe[3];     // edges queued by level-change pass k, at k % 3
     int mgt[3];                    // minimum support found by level-change pass k, at k % 3
     int dmin[2];                   // minimum decrement result above the level during level L_t, at t & 1
@@ -346,15 +345,15 @@ __device__ __forceinline__ void warp_append_staged(const PeelArgs& A, bool liste
 // the pass (0 at t = 0; afterwards the minimum support above L_{t-1} seen at
 // change t-1, lowered by every decrement result above L_{t-1} during level
 // L_{t-1}).  The pass compacts the survivors into list (t+1)&1, queues the
-// alive edges with support == g, collects those with support in (g, g+W) in
-// a side list, and takes the minimum support above g.  If anything was
-// queued, L_t = g.  Otherwise L_t = that minimum, and its frontier is found
-// in the side list (or, past the window, by one more pass over the compacted
-// list).  Every pass k ends with a grid barrier and writes its minimum,
-// side-list length and queued count to slot k % 3 of mgt / side_n / pfe; the
-// block-0 thread that clears slot (k+1) % 3 at the start of pass k clears a
-// slot that every block finished reading before the barrier of pass k-1.
-constexpr int kSideWindow = 64;
+// alive edges with support == g, and takes the minimum support above g.  If
+// anything was queued, L_t = g.  Otherwise L_t = that minimum, and one more
+// pass over the compacted list queues its frontier (3 of 307 level changes
+// at R-MAT scale 22; a side list of the supports just above g, written by
+// every first pass for that case, cost the level changes 3 ms there).  Every
+// pass k ends with a grid barrier and writes its minimum and queued count to
+// slot k % 3 of mgt / pfe; the block-0 thread that clears slot (k+1) % 3 at
+// the start of pass k clears a slot that every block finished reading before
+// the barrier of pass k-1.
 
 // Fold a per-lane minimum into *dst: one atomic per warp, skipped when *dst
 // is already no larger (a plain read keeps ten thousand warps from
@@ -413,7 +412,6 @@ constexpr int kStep = TDT_PEEL_STEP;
 __device__ __forceinline__ void pass_start(const PeelArgs& A, int np) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         A.ctl->mgt[(np + 1) % 3] = INT32_MAX;
-        A.ctl->side_n[(np + 1) % 3] = 0;
         A.ctl->pfe[(np + 1) % 3] = 0;
         A.ctl->passes++;
     }
@@ -435,28 +433,23 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
         const int32_t b = *(volatile int*)&A.ctl->dmin[(t + 1) & 1];
         g = a < b ? a : b;
     }
-    const int32_t gw_end = g > INT32_MAX - kSideWindow ? INT32_MAX : g + kSideWindow;
     const int slot = r_next & 3, buf = r_next % 3;
-    // buffer r_next + 1 = r_next - 2 is free: the dead bits of its items were
-    // set during round r_next - 1 (the finished round's items are still needed)
-    int2* side = reinterpret_cast<int2*>(A.qi[(r_next + 1) % 3]);
     AppendBuf B{app_e + (threadIdx.x / kWarp) * kAppBuf, 0, 0ull};
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         A.ctl->cnt[(t + 1) % 3] = 0;
         A.ctl->dmin[t & 1] = INT32_MAX;
     }
     pass_start(A, np);
-    // pass 1: compact, queue support == g, side-list the window, minimum above g.
-    // Blocks take tiles of kPeelWarps x kStep x 32 entries; each tile reserves
-    // its survivor and side-list ranges with one atomic each.
+    // pass 1: compact, queue support == g, minimum above g.  Blocks take
+    // tiles of kPeelWarps x kStep x 32 entries; each tile reserves its
+    // survivor range with one atomic.
     {
-        __shared__ int s_tk[kPeelWarps], s_tw[kPeelWarps];
-        __shared__ unsigned long long s_base[2];
+        __shared__ int s_tk[kPeelWarps];
+        __shared__ unsigned long long s_base;
         constexpr long long kTile = (long long)kPeelWarps * kStep * kWarp;
         const int wib = threadIdx.x / kWarp;
         int32_t mloc = INT32_MAX;
         unsigned long long* ocnt = &A.ctl->cnt[t % 3];
-        unsigned long long* scnt = &A.ctl->side_n[np % 3];
         const unsigned lt = lanemask_lt();
         for (long long tb = (long long)blockIdx.x * kTile; tb < ncur; tb += (long long)gridDim.x * kTile) {
             const long long base = tb + (long long)wib * (kStep * kWarp);
@@ -481,42 +474,28 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
                     keep[u] = ((cw >> ((unsigned)(e[u] & 7) * 4u)) & 15u) == kCodeAlive;
                 }
             }
-            unsigned km[kStep], wm[kStep];
-            int nk = 0, nwin = 0;
+            unsigned km[kStep];
+            int nk = 0;
 #pragma unroll
             for (int u = 0; u < kStep; u++) {
                 km[u] = __ballot_sync(kFull, keep[u]);
-                wm[u] = __ballot_sync(kFull, keep[u] && sv[u] > g && sv[u] < gw_end);
                 nk += __popc(km[u]);
-                nwin += __popc(wm[u]);
                 if (keep[u] && sv[u] > g) mloc = sv[u] < mloc ? sv[u] : mloc;
             }
-            if (lane == 0) {
-                s_tk[wib] = nk;
-                s_tw[wib] = nwin;
-            }
+            if (lane == 0) s_tk[wib] = nk;
             __syncthreads();
             if (wib == 0) {
-                const int a = lane < kPeelWarps ? s_tk[lane] : 0, b = lane < kPeelWarps ? s_tw[lane] : 0;
-                const int ai = warp_incl_scan(a), bi = warp_incl_scan(b);
-                if (lane == kPeelWarps - 1) {
-                    s_base[0] = ai ? atomicAdd(ocnt, (unsigned long long)ai) : 0ull;
-                    s_base[1] = bi ? atomicAdd(scnt, (unsigned long long)bi) : 0ull;
-                }
-                if (lane < kPeelWarps) {
-                    s_tk[lane] = ai - a;
-                    s_tw[lane] = bi - b;
-                }
+                const int a = lane < kPeelWarps ? s_tk[lane] : 0;
+                const int ai = warp_incl_scan(a);
+                if (lane == kPeelWarps - 1) s_base = ai ? atomicAdd(ocnt, (unsigned long long)ai) : 0ull;
+                if (lane < kPeelWarps) s_tk[lane] = ai - a;
             }
             __syncthreads();
-            unsigned long long ok = s_base[0] + (unsigned long long)s_tk[wib];
-            unsigned long long os = s_base[1] + (unsigned long long)s_tw[wib];
+            unsigned long long ok = s_base + (unsigned long long)s_tk[wib];
 #pragma unroll
             for (int u = 0; u < kStep; u++) {
                 if (keep[u]) nxt[ok + __popc(km[u] & lt)] = e[u];
-                if ((wm[u] >> lane) & 1u) side[os + __popc(wm[u] & lt)] = make_int2(e[u], sv[u]);
                 ok += __popc(km[u]);
-                os += __popc(wm[u]);
                 const bool want = keep[u] && sv[u] == g;
                 if (want) {
                     A.rnd[e[u]] = r_next;
@@ -541,29 +520,8 @@ __device__ __forceinline__ bool level_transition(const PeelArgs& A, bool listed,
     *l_out = m;
     pass_start(A, np);
     int32_t mloc = INT32_MAX;
-    if (m < gw_end) {
-        // pass 2a: the frontier is in the side list; edges outside it have
-        // support >= g + W, which bounds the next minimum from below
-        const long long ns = (long long)__ldcg(&A.ctl->side_n[(np + 2) % 3]);
-        mloc = gw_end;
-        for (long long base = gw * kWarp; base < ns; base += nw * kWarp) {
-            const long long i = base + lane;
-            int32_t e = 0, sv = INT32_MAX;
-            if (i < ns) {
-                const int2 x = __ldcg(side + i);
-                e = x.x;
-                sv = x.y;
-            }
-            const bool want = i < ns && sv == m;
-            if (!want && sv > m) mloc = sv < mloc ? sv : mloc;
-            if (want) {
-                A.rnd[e] = r_next;
-                code_mark(A.code, e, sv > 0 ? ((unsigned)r_next & 3u) : kCodeDead);
-            }
-            warp_append_staged(A, listed, slot, buf, want, e, sv, B, &A.ctl->pfe[np % 3]);
-        }
-    } else {
-        // pass 2b: one more pass over the compacted list
+    {
+        // pass 2: one more pass over the compacted list
         const long long n2 = (long long)__ldcg(&A.ctl->cnt[t % 3]);
         for (long long base = gw * kWarp; base < n2; base += nw * kWarp) {
             const long long i = base + lane;
