@@ -747,16 +747,16 @@ def bench_served_small(dev, srv, num_graphs=4096, rate=20000.0):
 # decomposition (T = 423,980,669) of this build.  The lists, the staging area
 # and the peel's slots all grow with T, so a phase's traffic at another size
 # is its rate x T.  Reported beside the algorithmic bytes, never used for them.
-TRAFFIC_PER_TRIANGLE = {"support": 41.2, "listing": 66.4, "peel": 60.5}
+TRAFFIC_PER_TRIANGLE = {"support": 41.2, "listing": 66.4, "peel": 46.6}
 TRAFFIC_SOURCE = ("ncu one-pass capture (dram__bytes_read.sum + dram__bytes_write.sum) of one R-MAT scale-20 "
                   "decomposition, scaled per triangle")
 # The same DRAM bytes per decomposition of R-MAT scale 22, edge factor 16,
 # from one-kernel, one-launch, one-pass captures of the main kernels at that
 # size (the one walk 130.8 GB, compaction 83.3 GB, transpose 56.2 GB, peel
-# 154.5 GB; the in-adjacency and bounds kernels scaled from scale 20): at
-# this size the peel's edge states no longer fit in L2, so its rate per
+# 121.4 GB; the in-adjacency and bounds kernels scaled from scale 20): at
+# this size the peel's supports no longer fit in L2, so its rate per
 # triangle is higher than at scale 20.
-TRAFFIC_BY_WORKLOAD = {(22, 16): {"support": 133.1e9, "listing": 139.5e9, "peel": 154.5e9}}
+TRAFFIC_BY_WORKLOAD = {(22, 16): {"support": 133.1e9, "listing": 139.5e9, "peel": 121.4e9}}
 TRAFFIC_SOURCE_BY_WORKLOAD = ("ncu one-kernel, one-launch, one-pass captures (dram__bytes_read.sum + "
                               "dram__bytes_write.sum) of the main kernels of one decomposition of this workload")
 
