@@ -1177,14 +1177,22 @@ __global__ void list_decide_kernel(const int64_t* __restrict__ off, const int64_
 // flat index space (lane-held exclusive starts S), each lane finds the edge
 // of its entry by a 5-step search over S (shuffles), and four 32-entry
 // windows are copied per step so four loads per lane are in flight.
-__global__ void stage_compact_kernel(const int64_t* __restrict__ soff, const int32_t* __restrict__ bnd,
+#ifndef TDT_CMP_WIN
+#define TDT_CMP_WIN 4
+#endif
+#ifndef TDT_CMP_MINB
+#define TDT_CMP_MINB 6
+#endif
+constexpr int kCmpBlock = 256;
+__global__ void __launch_bounds__(kCmpBlock, TDT_CMP_MINB)
+stage_compact_kernel(const int64_t* __restrict__ soff, const int32_t* __restrict__ bnd,
                                      const int32_t* __restrict__ cA, const int32_t* __restrict__ cB,
                                      const int64_t* __restrict__ off, const int2* __restrict__ stage_end,
                                      int2* __restrict__ lists, int64_t E, const PeelCtl* ctl) {
     if (*(volatile const int*)&ctl->compact_skip) return;
     const unsigned lane = lane_id();
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    constexpr int kWin = 4;
+    constexpr int kWin = TDT_CMP_WIN;
     for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kWarp; base < E;
          base += nw * kWarp) {
         const int64_t e = base + lane;
@@ -1579,8 +1587,14 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     if (rc) return rc;
     list_decide_kernel<<<1, 1, 0, st>>>(L.off, L.soff, E, tail, tail > 0, L.ctl);
     TDT_LAUNCH_CHECK("list_decide");
-    stage_compact_kernel<<<grid_for(E * 32, tb, di.sms, 8), tb, 0, st>>>(L.soff, L.bnd, cA, cB, L.off, stage_end,
-                                                                           lists, E, L.ctl);
+    {
+        // one wave of resident blocks (the loop is grid-strided)
+        int occ_c = 0;
+        TDT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, stage_compact_kernel, kCmpBlock, 0));
+        if (occ_c < 1) occ_c = 1;
+        const unsigned g_c = grid_for(E * 32, kCmpBlock, di.sms, occ_c);
+        stage_compact_kernel<<<g_c, kCmpBlock, 0, st>>>(L.soff, L.bnd, cA, cB, L.off, stage_end, lists, E, L.ctl);
+    }
     TDT_LAUNCH_CHECK("stage_compact");
     // second walk, when the lists fit but not beside the staging area
     list_cursor_kernel<<<g_e, tb, 0, st>>>(L.off, cA, E, curA, curB, L.ctl);
