@@ -67,6 +67,9 @@ constexpr int kSlBV = kSlVI + 4 * kWarp;
 constexpr int kSlBm = kSlBV + 8 * kWarp;
 constexpr int kSlQ = kSlBm + (1 << kLightBmLog2) / 8;
 static_assert(kSlQ + 8 * kQueue <= kSliceBytes, "light slice");
+// a push adds up to 32 candidates to a queue holding up to 31 (it is drained
+// to below 32 after every push)
+static_assert(kQueue >= 2 * kWarp, "candidate queue");
 
 // Heavy rows: one block, the whole buffer:
 //   su[H] | cnt[H] | group S[512] VI[512] BV[512] | bitmap 2^16 bits | queues
