@@ -353,14 +353,20 @@ __device__ __forceinline__ void walk_group_vec(const OutRows<Off>& G, const SupA
             p0 = ((lo >> 2) + (c - SC[o])) << 2;
             const int4 w4 = __ldg(cols4 + (p0 >> 2));
             const int32_t wq[4] = {w4.x, w4.y, w4.z, w4.w};
+            // the chunk's entries inside [lo, hi): a mask, once per chunk
+            unsigned vm = 0xFu;
+            if (p0 < lo) vm &= 0xFu << (lo - p0);
+            if (p0 + 4 > hi) vm &= 0xFu >> (p0 + 4 - hi);
+            // every entry is tested (a hashed index stays inside the bitmap)
+            // and the mask applied after
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int32_t w = wq[q];
-                if (p0 + q >= lo && p0 + q < hi && w <= R.umax) {
-                    const uint32_t h = bm_hash(w, R.bm_log2);
-                    cm |= ((R.bm[h >> 5] >> (h & 31)) & 1u) << q;
-                }
+                const uint32_t h = bm_hash(w, R.bm_log2);
+                const unsigned hit = (R.bm[h >> 5] >> (h & 31)) & (w <= R.umax ? 1u : 0u);
+                cm |= hit << q;
             }
+            cm &= vm;
             vi = VI[o];
         }
         ob += nb + (Bn == base + kWarp ? 1 : 0);
