@@ -148,7 +148,14 @@ struct SupCtl {
     unsigned long long light_next;
 };
 
+#ifndef TDT_BM_LOWBITS
+#define TDT_BM_LOWBITS 1
+#endif
+// Bitmap index of vertex id w: its low bits (ids are degree ranks, and a
+// row's out-neighbours cluster among the high ranks, so consecutive ids land
+// on distinct bits), or a multiplicative hash.
 __device__ __forceinline__ uint32_t bm_hash(int32_t w, int log2bits) {
+    if (TDT_BM_LOWBITS) return (uint32_t)w & ((1u << log2bits) - 1u);
     return ((uint32_t)w * 0x9E3779B1u) >> (32 - log2bits);
 }
 
