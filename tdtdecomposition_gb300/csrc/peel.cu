@@ -35,7 +35,10 @@
 
 namespace tdt {
 
-constexpr int kPeelBlock = 512;
+#ifndef TDT_PEEL_BLOCK
+#define TDT_PEEL_BLOCK 512
+#endif
+constexpr int kPeelBlock = TDT_PEEL_BLOCK;
 constexpr int kPeelWarps = kPeelBlock / kWarp;
 constexpr int kItemBits = 28;
 constexpr int kCandBits = 36;
@@ -738,20 +741,24 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
 // their decrements (INT32_MIN: no decrement).  An edge whose support fell to
 // l is marked for sub-round r+1 and queued; a larger result lowers the bound
 // dm of the next level.
+#ifndef TDT_PEEL_WIN
+#define TDT_PEEL_WIN 2
+#endif
+constexpr int kWin = TDT_PEEL_WIN;  // 32-slot windows per peel step
 struct Pending {
-    int32_t e[4];
-    int32_t o[4];
+    int32_t e[2 * kWin];
+    int32_t o[2 * kWin];
 };
 
 template <bool Listed>
 __device__ __forceinline__ void settle(const PeelArgs& A, const Pending& P, int r, int32_t l, int nslot, int nbuf,
                                        AppendBuf& B, int32_t& dm) {
-    bool w[4];
+    bool w[2 * kWin];
     // queued with an item when the level is above 0 (an edge without
     // triangles never appears in a list, so its code is never read)
     const unsigned cm = l > 0 ? ((unsigned)(r + 1) & 3u) : kCodeDead;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < 2 * kWin; j++) {
         w[j] = P.o[j] == l + 1;
         if (P.o[j] > l + 1) dm = P.o[j] - 1 < dm ? P.o[j] - 1 : dm;
         if (w[j]) {
@@ -759,12 +766,14 @@ __device__ __forceinline__ void settle(const PeelArgs& A, const Pending& P, int 
             code_mark(A.code, P.e[j], cm);
         }
     }
-    if (Listed) {
-        warp_append2_staged<Listed>(A, nslot, nbuf, w[0], P.e[0], w[1], P.e[1], l, B, &A.ctl->fe[nslot]);
-        warp_append2_staged<Listed>(A, nslot, nbuf, w[2], P.e[2], w[3], P.e[3], l, B, &A.ctl->fe[nslot]);
-    } else {
-        warp_append2_direct<Listed>(A, nslot, nbuf, w[0], P.e[0], w[1], P.e[1], l, &A.ctl->fe[nslot]);
-        warp_append2_direct<Listed>(A, nslot, nbuf, w[2], P.e[2], w[3], P.e[3], l, &A.ctl->fe[nslot]);
+#pragma unroll
+    for (int h = 0; h < kWin; h++) {
+        if (Listed)
+            warp_append2_staged<Listed>(A, nslot, nbuf, w[2 * h], P.e[2 * h], w[2 * h + 1], P.e[2 * h + 1], l, B,
+                                        &A.ctl->fe[nslot]);
+        else
+            warp_append2_direct<Listed>(A, nslot, nbuf, w[2 * h], P.e[2 * h], w[2 * h + 1], P.e[2 * h + 1], l,
+                                        &A.ctl->fe[nslot]);
     }
 }
 
@@ -807,13 +816,14 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     // kDynChunk slots from a shared cursor (the binary search of a slot costs
     // from one load to twenty, so equal ranges finish far apart).
     const bool dyn = !Listed && kDynChunk > 0 && T >= A.dyn_min_slots;
-    const long long per_warp = (((T + nwarps - 1) / nwarps) + 63) & ~63ll;
+    constexpr long long kStepSlots = (long long)kWin * kWarp;
+    const long long per_warp = (((T + nwarps - 1) / nwarps) + kStepSlots - 1) / kStepSlots * kStepSlots;
     long long cb0 = gwarp * per_warp;
     long long cb1 = cb0 + per_warp < T ? cb0 + per_warp : T;
     if (!dyn && cb0 >= cb1) return;
     Pending P;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < 2 * kWin; j++) {
         P.e[j] = 0;
         P.o[j] = INT32_MIN;
     }
@@ -845,93 +855,103 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     long long nst = i0 + 1 < N ? __ldcg(qb + i0 + 1) : LLONG_MAX;
     int4 rec = __ldcg(qi + i0);
     bool rv = true;
-    for (long long cb = cb0; cb < cb1; cb += 2 * kWarp) {
-        const long long cb2 = cb + kWarp;
-        const bool has_b = cb2 < cb1;
-        const long long ta = cb + lane, tb = cb2 + lane;
-        const bool va = ta < cb1, vb = has_b && tb < cb1;
-        int4 ita, itb = make_int4(0, 0, 0, 0);
-        long long bla, blb = 0;
-        window_items(qb, qi, N, cb, va, le, i0, base0, nst, rec, rv, ita, bla);
-        if (has_b) window_items(qb, qi, N, cb2, vb, le, i0, base0, nst, rec, rv, itb, blb);
-        int32_t fa = 0, ga = 0, fb = 0, gb = 0;
-        bool tra = false, trb = false;
-        if (va) tra = slot_edges<Listed>(A, ita, ta - bla, fa, ga);
-        if (vb) trb = slot_edges<Listed>(A, itb, tb - blb, fb, gb);
-        int32_t rfa = -2, rga = -2, rfb = -2, rgb = -2;
+    for (long long cb = cb0; cb < cb1; cb += kStepSlots) {
+        int4 it[kWin];
+        long long bl[kWin];
+        bool v[kWin];
+#pragma unroll
+        for (int h = 0; h < kWin; h++) {
+            const long long cbh = cb + h * kWarp;
+            it[h] = make_int4(0, 0, 0, 0);
+            bl[h] = 0;
+            v[h] = cbh + lane < cb1;
+            if (cbh < cb1) window_items(qb, qi, N, cbh, v[h], le, i0, base0, nst, rec, rv, it[h], bl[h]);
+        }
+        int32_t f[kWin], g[kWin];
+        bool tr[kWin];
+#pragma unroll
+        for (int h = 0; h < kWin; h++) {
+            f[h] = 0;
+            g[h] = 0;
+            tr[h] = false;
+            if (v[h]) tr[h] = slot_edges<Listed>(A, it[h], cb + h * kWarp + lane - bl[h], f[h], g[h]);
+        }
+        int32_t rf[kWin], rg[kWin];
+#pragma unroll
+        for (int h = 0; h < kWin; h++) rf[h] = rg[h] = -2;
         if (kPeelCodes) {
             // the partners' round codes (L2): dead, alive, peeling now, marked
-            unsigned xa = 0, ya = 0, xb = 0, yb = 0;
-            if (tra) {
-                xa = __ldcg(A.code + (fa >> 3));
-                ya = __ldcg(A.code + (ga >> 3));
-            }
-            if (trb) {
-                xb = __ldcg(A.code + (fb >> 3));
-                yb = __ldcg(A.code + (gb >> 3));
+            unsigned x[kWin], y[kWin];
+#pragma unroll
+            for (int h = 0; h < kWin; h++) {
+                x[h] = y[h] = 0;
+                if (tr[h]) {
+                    x[h] = __ldcg(A.code + (f[h] >> 3));
+                    y[h] = __ldcg(A.code + (g[h] >> 3));
+                }
             }
             // the previous step's decrement results, while these loads are in flight
             if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
-            if (tra) {
-                rfa = code_round(xa, fa, r);
-                rga = code_round(ya, ga, r);
-            }
-            if (trb) {
-                rfb = code_round(xb, fb, r);
-                rgb = code_round(yb, gb, r);
+#pragma unroll
+            for (int h = 0; h < kWin; h++) {
+                if (tr[h]) {
+                    rf[h] = code_round(x[h], f[h], r);
+                    rg[h] = code_round(y[h], g[h], r);
+                }
             }
         } else {
             // dead-bit filter: a triangle with an edge peeled before round r is gone
             if (kDeadFilter) {
-                unsigned xa = 0, ya = 0, xb = 0, yb = 0;
-                if (tra) {
-                    xa = A.dead[fa >> 5];
-                    ya = A.dead[ga >> 5];
+                unsigned x[kWin], y[kWin];
+#pragma unroll
+                for (int h = 0; h < kWin; h++) {
+                    x[h] = y[h] = 0;
+                    if (tr[h]) {
+                        x[h] = A.dead[f[h] >> 5];
+                        y[h] = A.dead[g[h] >> 5];
+                    }
                 }
-                if (trb) {
-                    xb = A.dead[fb >> 5];
-                    yb = A.dead[gb >> 5];
+#pragma unroll
+                for (int h = 0; h < kWin; h++)
+                    if (tr[h] && (((x[h] >> (f[h] & 31)) | (y[h] >> (g[h] & 31))) & 1u)) tr[h] = false;
+            }
+#pragma unroll
+            for (int h = 0; h < kWin; h++) {
+                if (tr[h]) {
+                    rf[h] = __ldcg(A.rnd + f[h]);
+                    rg[h] = __ldcg(A.rnd + g[h]);
                 }
-                if (tra && (((xa >> (fa & 31)) | (ya >> (ga & 31))) & 1u)) tra = false;
-                if (trb && (((xb >> (fb & 31)) | (yb >> (gb & 31))) & 1u)) trb = false;
-            }
-            if (tra) {
-                rfa = __ldcg(A.rnd + fa);
-                rga = __ldcg(A.rnd + ga);
-            }
-            if (trb) {
-                rfb = __ldcg(A.rnd + fb);
-                rgb = __ldcg(A.rnd + gb);
             }
             // the previous step's decrement results, while these loads are in flight
             if (kPeelDefer) settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
         }
         // a triangle is alive when both other edges are alive or peel in r or r+1;
         // which of f, g this lane decrements: the ownership rules above
-        bool dfa = false, dga = false, dfb = false, dgb = false;
-        if (tra && (rfa == -1 || rfa >= r) && (rga == -1 || rga >= r)) {
-            const bool ff = rfa == r, fg = rga == r;
-            dfa = !ff && (!fg || ita.x < ga) && (!kSkipMarked || rfa != r + 1);
-            dga = !fg && (!ff || ita.x < fa) && (!kSkipMarked || rga != r + 1);
-        }
-        if (trb && (rfb == -1 || rfb >= r) && (rgb == -1 || rgb >= r)) {
-            const bool ff = rfb == r, fg = rgb == r;
-            dfb = !ff && (!fg || itb.x < gb) && (!kSkipMarked || rfb != r + 1);
-            dgb = !fg && (!ff || itb.x < fb) && (!kSkipMarked || rgb != r + 1);
+        bool df[kWin], dg[kWin];
+#pragma unroll
+        for (int h = 0; h < kWin; h++) {
+            df[h] = dg[h] = false;
+            if (tr[h] && (rf[h] == -1 || rf[h] >= r) && (rg[h] == -1 || rg[h] >= r)) {
+                const bool ff = rf[h] == r, fg = rg[h] == r;
+                df[h] = !ff && (!fg || it[h].x < g[h]) && (!kSkipMarked || rf[h] != r + 1);
+                dg[h] = !fg && (!ff || it[h].x < f[h]) && (!kSkipMarked || rg[h] != r + 1);
+            }
         }
         // issue all decrements; their results are used by the next step
-        P.e[0] = fa;
-        P.e[1] = ga;
-        P.e[2] = fb;
-        P.e[3] = gb;
-        P.o[0] = dfa ? atomicSub(A.live + fa, 1) : INT32_MIN;
-        P.o[1] = dga ? atomicSub(A.live + ga, 1) : INT32_MIN;
-        P.o[2] = dfb ? atomicSub(A.live + fb, 1) : INT32_MIN;
-        P.o[3] = dgb ? atomicSub(A.live + gb, 1) : INT32_MIN;
+#pragma unroll
+        for (int h = 0; h < kWin; h++) {
+            P.e[2 * h] = f[h];
+            P.e[2 * h + 1] = g[h];
+        }
+#pragma unroll
+        for (int h = 0; h < kWin; h++) {
+            P.o[2 * h] = df[h] ? atomicSub(A.live + f[h], 1) : INT32_MIN;
+            P.o[2 * h + 1] = dg[h] ? atomicSub(A.live + g[h], 1) : INT32_MIN;
+        }
         if (!kPeelDefer) {
             settle<Listed>(A, P, r, l, nslot, nbuf, B, dm);
 #pragma unroll
-            for (int j = 0; j < 4; j++) P.o[j] = INT32_MIN;
+            for (int j = 0; j < 2 * kWin; j++) P.o[j] = INT32_MIN;
         }
     }
     if (!dyn) break;
