@@ -51,8 +51,13 @@ constexpr int kTrSmemCur = 3072;   // out-edge cursors a group keeps in shared m
 #define TDT_TR_KEYED 1
 #endif
 constexpr int kTrKeys = TDT_TR_KEYED ? kTrSmemCur : 0;  // out-edges of a keyed group (bases reuse s_cur)
-constexpr int kTrChunkPer = 2;                           // entries per thread per keyed chunk
+#ifndef TDT_TR_CHUNK_PER
+#define TDT_TR_CHUNK_PER 4
+#endif
+constexpr int kTrChunkPer = TDT_TR_CHUNK_PER;                           // entries per thread per keyed chunk (counts stay below 2^16)
 constexpr int kTrChunk = kTrBlock * kTrChunkPer;
+static_assert(kTrChunk < 65536 && kTrSmemCur <= 65536 && kTrSmemCur % 2 == 0,
+              "16-bit per-edge counters and touched-edge indices");
 
 struct TrArgs {
     const int64_t* cp;                  // in-adjacency offsets (cp[V] = E)
