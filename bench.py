@@ -752,11 +752,11 @@ TRAFFIC_SOURCE = ("ncu one-pass capture (dram__bytes_read.sum + dram__bytes_writ
                   "decomposition, scaled per triangle")
 # The same DRAM bytes per decomposition of R-MAT scale 22, edge factor 16,
 # from one-kernel, one-launch, one-pass captures of the main kernels at that
-# size (the one walk 130.8 GB, compaction 82.7 GB, transpose 56.2 GB, peel
+# size (the one walk 130.8 GB, compaction 82.7 GB, transpose 56.0 GB, peel
 # 121.3 GB; the in-adjacency and bounds kernels scaled from scale 20): at
 # this size the peel's supports no longer fit in L2, so its rate per
 # triangle is higher than at scale 20.
-TRAFFIC_BY_WORKLOAD = {(22, 16): {"support": 133.1e9, "listing": 138.9e9, "peel": 121.3e9}}
+TRAFFIC_BY_WORKLOAD = {(22, 16): {"support": 133.1e9, "listing": 138.7e9, "peel": 121.3e9}}
 TRAFFIC_SOURCE_BY_WORKLOAD = ("ncu one-kernel, one-launch, one-pass captures (dram__bytes_read.sum + "
                               "dram__bytes_write.sum) of the main kernels of one decomposition of this workload")
 
