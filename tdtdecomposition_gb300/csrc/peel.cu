@@ -30,6 +30,8 @@
 // per warp: item count in the high bits, candidate count in the low bits, so
 // item order equals slot order), and every lane of the grid takes one slot
 // per step.  Hub edges therefore spread over all SMs instead of one thread.
+// With per-edge triangle lists (listed mode) a slot is one list entry: the
+// two partner edges, whose states come from 4-bit round codes held in L2.
 #include "common.cuh"
 #include "sort.cuh"
 
@@ -89,9 +91,9 @@ struct PeelArgs {
     int4* qi[3];
     long long* qb[3];
     int32_t* alive[2];    // compacted alive-edge lists (level transitions)
-    // bit e set: edge e was peeled in a sub-round before the current one (a
-    // filter in L2 that keeps most dead triangles away from the edge states;
-    // a bit not set yet only costs the state check it would have saved)
+    // bit e set: edge e was peeled in a sub-round before the current one (the
+    // search peel's filter in L2 before a candidate's binary search; a bit not
+    // set yet only costs the search it would have saved)
     unsigned* dead;
     // round code of edge e in the 4 bits at (e & 7) * 4 of word e >> 3 (the
     // listed peel's partner-state check; see code_round)
