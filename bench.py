@@ -226,7 +226,7 @@ def bench_batched(dev, steps, warmup, num_graphs=4096):
     bt = B.batch_from_union(g, eo, vo)
     E = g.num_edges
     wsb = T.Workspace(dev)
-    tuned = autotune.tune(g, workspace=wsb)
+    tuned = autotune.tune(g, workspace=wsb)  # (warp_cap, heavy_cap, lists, peel_grid, vec)
     for _ in range(warmup):
         B.decompose(bt, workspace=wsb, lists=tuned[2], sync=False)
     torch.cuda.synchronize()
@@ -283,7 +283,8 @@ def bench_batched(dev, steps, warmup, num_graphs=4096):
             "kmax_max": int(ref.kmax.max()), "sub_rounds": ref.union.rounds,
             "cuda_graph": {"ms_per_step": ms_graph, "value": E / (ms_graph / 1e3),
                            "note": "support, listing, the cooperative peel and outputs captured once, replayed"},
-            "autotuned": {"warp_cap": tuned[0], "heavy_cap": tuned[1], "lists": tuned[2]},
+            "autotuned": {"warp_cap": tuned[0], "heavy_cap": tuned[1], "lists": tuned[2],
+                          "peel_grid_half_sms": tuned[3], "vector_walk": tuned[4]},
             "host_generation_s": t_gen, "results_identical_to_plain": True}
 
 

@@ -93,6 +93,15 @@ void tdt_set_vector_walk(int on);
  * launched afterwards from any thread. */
 void tdt_set_bulk_staging(int on);
 
+/* Knob of the persistent peel (no counterpart in the reference): its grid in
+ * units of half the SM count (1 = one block per two SMs, 2 = one per SM, 4 =
+ * two per SM, capped by what stays resident); 0 (the default) restores the
+ * size heuristic (half the SMs under 2^18 edges with lists, one block per SM
+ * under 2^22, otherwise every resident block).  The autotuner's launch-shape
+ * dimension.  Results do not depend on it.  Affects calls launched
+ * afterwards from any thread. */
+void tdt_set_peel_grid(int half_sms);
+
 /* Testing knobs of the failure paths (no counterpart in the reference, which
  * has no bounded waits).  tdt_set_peel_deadline_ns: wall-clock budget of the
  * peel launches that follow (<= 0 restores the default of 120 s); a run past

@@ -31,6 +31,7 @@ _SIGS = [
     ("tdt_set_support_caps", None, [ctypes.c_int, ctypes.c_int]),
     ("tdt_set_vector_walk", None, [ctypes.c_int]),
     ("tdt_set_bulk_staging", None, [ctypes.c_int]),
+    ("tdt_set_peel_grid", None, [ctypes.c_int]),
     ("tdt_set_peel_deadline_ns", None, [ctypes.c_longlong]),
     ("tdt_set_ktruss_batch_caps", None, [ctypes.c_longlong, ctypes.c_longlong]),
     ("tdt_set_peel_dynamic_min", None, [ctypes.c_longlong]),

@@ -122,6 +122,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
 void set_support_caps(int warp_cap, int heavy_cap);
 void set_vector_walk(int on);
 void set_bulk_staging(int on);
+void set_peel_grid(int half_sms);
 void set_peel_deadline(long long ns);
 void set_fixed_caps(long long items, long long cands);
 void set_peel_dyn_min(long long slots);
@@ -168,6 +169,7 @@ API unsigned long long tdt_launch_count(void) { return __atomic_load_n(&g_launch
 API void tdt_set_support_caps(int warp_cap, int heavy_cap) { set_support_caps(warp_cap, heavy_cap); }
 API void tdt_set_vector_walk(int on) { set_vector_walk(on); }
 API void tdt_set_bulk_staging(int on) { set_bulk_staging(on); }
+API void tdt_set_peel_grid(int half_sms) { set_peel_grid(half_sms); }
 API void tdt_set_peel_deadline_ns(long long ns) { set_peel_deadline(ns); }
 API void tdt_set_ktruss_batch_caps(long long items, long long cands) { set_fixed_caps(items, cands); }
 API void tdt_set_peel_dynamic_min(long long slots) { set_peel_dyn_min(slots); }

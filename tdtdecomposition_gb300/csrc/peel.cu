@@ -1386,6 +1386,10 @@ int peel_clock(const void* ws, long long* ns, cudaStream_t st) {
     return TDT_OK;
 }
 void set_peel_dyn_min(long long slots) { g_dyn_min_slots = slots; }
+// Peel grid in half-SM units (0: the size heuristic below); the autotuner's
+// launch-shape dimension.
+static int g_peel_half_sms = 0;
+void set_peel_grid(int half_sms) { g_peel_half_sms = half_sms > 0 ? half_sms : 0; }
 static long long g_fixed_item_cap = 0, g_fixed_cand_cap = 0;
 void set_fixed_caps(long long items, long long cands) {
     g_fixed_item_cap = items;
@@ -1671,6 +1675,7 @@ int run_peel(int mode, const int32_t* rows, const int32_t* cols, const int64_t* 
     int nblk = di.sms * occ;
     if (tail > 0 && E < (1ll << 18)) nblk = (di.sms + 1) / 2;
     else if (tail > 0 && E < (1ll << 22)) nblk = di.sms;
+    if (g_peel_half_sms > 0) nblk = (g_peel_half_sms * di.sms + 1) / 2;
     if (nblk > di.sms * occ) nblk = di.sms * occ;
     dim3 grid(nblk), block(kPeelBlock);
     void* args[] = {&A};

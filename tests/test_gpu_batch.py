@@ -70,10 +70,19 @@ def test_autotune_picks_a_split_and_keeps_results():
                rows=torch.as_tensor(rows).cuda())
     ref = T.truss_decompose(g, lists=False)
     try:
-        wc, hc, lists = autotune.tune(g)
-        assert (wc, hc) in autotune.CANDIDATES
-        got = T.truss_decompose(g, lists=lists)
+        cfg = autotune.tune(g)
+        assert (cfg.warp_cap, cfg.heavy_cap) in autotune.CANDIDATES
+        assert cfg.peel_grid in autotune.PEEL_GRIDS and cfg.vec in autotune.VEC_WALK
+        got = T.truss_decompose(g, lists=cfg.lists)
         assert torch.equal(got.truss, ref.truss) and torch.equal(got.e_truss, ref.e_truss)
+        # every peel grid and walk width gives the same result
+        for pg in autotune.PEEL_GRIDS:
+            for vec in autotune.VEC_WALK:
+                autotune.apply(autotune.Config(cfg.warp_cap, cfg.heavy_cap, cfg.lists, pg, vec))
+                got = T.truss_decompose(g, lists=cfg.lists)
+                assert torch.equal(got.truss, ref.truss) and torch.equal(got.e_truss, ref.e_truss), (pg, vec)
+        # a cached workload answers without timing
+        assert autotune.tune(g) == cfg
     finally:
         autotune.reset()
 
