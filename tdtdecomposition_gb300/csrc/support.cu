@@ -70,6 +70,9 @@ static_assert(kSlQ + 8 * kQueue <= kSliceBytes, "light slice");
 // a push adds up to 32 candidates to a queue holding up to 31 (it is drained
 // to below 32 after every push)
 static_assert(kQueue >= 2 * kWarp, "candidate queue");
+// the vectorised walk keeps a group as int4 {SC, BV, HI, VI} over S|VI|BV|HI
+static_assert(kSlS % 16 == 0 && kSlVI == kSlS + 4 * kWarp && kSlBV == kSlVI + 4 * kWarp && kSlBm >= kSlS + 16 * kWarp,
+              "light group layout");
 
 // Heavy rows: one block, the whole buffer:
 //   su[H] | cnt[H] | group S[512] VI[512] BV[512] | bitmap 2^16 bits | queues
@@ -85,6 +88,8 @@ constexpr int kHvVI = kHvBV - 4 * kSeg;
 constexpr int kHvS = kHvVI - 4 * kSeg;
 constexpr int kHeavyCap = kHvS / 8;            // su + cnt, 8 bytes per entry
 static_assert(kHeavyCap >= 4096, "heavy cap");
+static_assert(kHvS % 16 == 0 && kHvVI == kHvS + 4 * kSeg && kHvBV == kHvVI + 4 * kSeg && kHvBm >= kHvS + 16 * kSeg,
+              "heavy group layout");
 static_assert((1 << kHugeBmLog2) / 8 <= kHvS, "in-place bitmap");
 static_assert(kHeavyCap < 65536, "packed 16-bit role counters");
 
@@ -332,20 +337,21 @@ __device__ __forceinline__ void walk_group(const OutRows<Off>& G, const SupArgs&
 // that hold it, so a chunk belongs to one v and comes with one int4 load; the
 // widened ends are masked by [BV[k], HI[k]).  SC[0..n) are the strictly
 // increasing chunk starts of the group's lists in the flat chunk space, c0 a
-// multiple of 32 and o0 the group entry that holds chunk c0.  One owner
+// multiple of 32 and o0 the group entry that holds chunk c0.  The group is
+// one int4 per list, GE[k] = {SC[k], BV[k], HI[k], VI[k]}: a lane reads its
+// list's entry with one shared-memory load.  One owner
 // reduction serves 128 wedges instead of 32.  cols must be 16-byte aligned
 // (a 16-byte chunk never crosses a page, so the widened reads stay mapped).
 template <int M, bool kIdOrdered, class Off>
 __device__ __forceinline__ void walk_group_vec(const OutRows<Off>& G, const SupArgs& A, const RowState& R,
-                                               const int32_t* SC, const int32_t* VI, const int32_t* BV,
-                                               const int32_t* HI, int n, int c0, int c1, int o0, WarpQueue& Q) {
+                                               const int4* GE, int n, int c0, int c1, int o0, WarpQueue& Q) {
     const unsigned lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int4* __restrict__ cols4 = reinterpret_cast<const int4*>(G.cols);
     int ob = o0;
     for (int base = c0; base < c1; base += kWarp) {
         const int k = ob + 1 + (int)lane;
-        const int32_t B = k < n ? SC[k] : INT32_MAX;
+        const int32_t B = k < n ? GE[k].x : INT32_MAX;
         const unsigned bit = ((unsigned)(B - base) < (unsigned)kWarp) ? (1u << (B - base)) : 0u;
         const unsigned mk = __reduce_or_sync(kFull, bit);
         const int nb = __popc(mk);
@@ -356,8 +362,9 @@ __device__ __forceinline__ void walk_group_vec(const OutRows<Off>& G, const SupA
         int vi = 0;
         if (c < c1) {
             const int o = ob + __popc(mk & (lt | (1u << lane)));
-            const int32_t lo = BV[o], hi = HI[o];
-            p0 = ((lo >> 2) + (c - SC[o])) << 2;
+            const int4 ge = GE[o];
+            const int32_t lo = ge.y, hi = ge.z;
+            p0 = ((lo >> 2) + (c - ge.x)) << 2;
             const int4 w4 = __ldg(cols4 + (p0 >> 2));
             const int32_t wq[4] = {w4.x, w4.y, w4.z, w4.w};
             // the chunk's entries inside [lo, hi): a mask, once per chunk
@@ -374,7 +381,7 @@ __device__ __forceinline__ void walk_group_vec(const OutRows<Off>& G, const SupA
                 cm |= hit << q;
             }
             cm &= vm;
-            vi = VI[o];
+            vi = ge.w;
         }
         ob += nb + (Bn == base + kWarp ? 1 : 0);
         if (__any_sync(kFull, cm != 0)) {
@@ -637,6 +644,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
         int32_t* g_VI = reinterpret_cast<int32_t*>(smem + kHvVI);
         int32_t* g_BV = reinterpret_cast<int32_t*>(smem + kHvBV);
         int32_t* g_HI = g_BV + kSeg;  // list ends (the vectorised walk)
+        int4* g_GE = reinterpret_cast<int4*>(smem + kHvS);  // the vectorised walk's layout of the same area
         WarpQueue Q;
         Q.pos = reinterpret_cast<int32_t*>(smem + kHvQueues + wib * 8 * kQueue);
         Q.vi = Q.pos + kQueue;
@@ -705,10 +713,14 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                     __syncthreads();
                     if (len > 0) {
                         const int ci = s_wsum[1][wib] + __popc(nem & lanemask_lt());
-                        g_S[ci] = s_wsum[0][wib] + incl - units;
-                        g_VI[ci] = i;
-                        g_BV[ci] = bv;
-                        g_HI[ci] = bv + len;
+                        if (kVec) {
+                            g_GE[ci] = make_int4(s_wsum[0][wib] + incl - units, bv, bv + len, i);
+                        } else {
+                            g_S[ci] = s_wsum[0][wib] + incl - units;
+                            g_VI[ci] = i;
+                            g_BV[ci] = bv;
+                            g_HI[ci] = bv + len;
+                        }
                     }
                     const int total = s_wsum[0][kSupWarps];
                     const int n = s_wsum[1][kSupWarps];
@@ -723,12 +735,12 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                             int lo = 0, hi = n - 1;  // last entry with S <= w0
                             while (lo < hi) {
                                 const int mid = (lo + hi + 1) >> 1;
-                                if (g_S[mid] <= w0) lo = mid; else hi = mid - 1;
+                                if ((kVec ? g_GE[mid].x : g_S[mid]) <= w0) lo = mid; else hi = mid - 1;
                             }
                             o0 = lo;
                         }
                         o0 = __shfl_sync(kFull, o0, 0);
-                        if (kVec) walk_group_vec<M, kIdOrdered>(G, A, R, g_S, g_VI, g_BV, g_HI, n, w0, w1, o0, Q);
+                        if (kVec) walk_group_vec<M, kIdOrdered>(G, A, R, g_GE, n, w0, w1, o0, Q);
                         else walk_group<M, kIdOrdered>(G, A, R, g_S, g_VI, g_BV, n, w0, w1, o0, Q);
                     }
                     __syncthreads();  // the group arrays are rewritten next
@@ -750,6 +762,7 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
     int32_t* l_VI = reinterpret_cast<int32_t*>(sl + kSlVI);
     int32_t* l_BV = reinterpret_cast<int32_t*>(sl + kSlBV);
     int32_t* l_HI = l_BV + kWarp;  // list ends (the vectorised walk)
+    int4* l_GE = reinterpret_cast<int4*>(sl + kSlS);  // the vectorised walk's layout of the same area
     uint32_t* l_bm = reinterpret_cast<uint32_t*>(sl + kSlBm);
     WarpQueue Q;
     Q.pos = reinterpret_cast<int32_t*>(sl + kSlQ);
@@ -799,14 +812,18 @@ __global__ void __launch_bounds__(kSupBlock, kSupMinBlocks) support_kernel(OutRo
                 const int total = __shfl_sync(kFull, incl, 31);
                 if (len > 0) {
                     const int ci = __popc(nem & lanemask_lt());
-                    l_S[ci] = incl - units;
-                    l_VI[ci] = i;
-                    l_BV[ci] = bv;
-                    l_HI[ci] = bv + len;
+                    if (kVec) {
+                        l_GE[ci] = make_int4(incl - units, bv, bv + len, i);
+                    } else {
+                        l_S[ci] = incl - units;
+                        l_VI[ci] = i;
+                        l_BV[ci] = bv;
+                        l_HI[ci] = bv + len;
+                    }
                 }
                 __syncwarp();
                 if (total > 0) {
-                    if (kVec) walk_group_vec<M, kIdOrdered>(G, A, R, l_S, l_VI, l_BV, l_HI, __popc(nem), 0, total, 0, Q);
+                    if (kVec) walk_group_vec<M, kIdOrdered>(G, A, R, l_GE, __popc(nem), 0, total, 0, Q);
                     else walk_group<M, kIdOrdered>(G, A, R, l_S, l_VI, l_BV, __popc(nem), 0, total, 0, Q);
                 }
                 __syncwarp();
