@@ -48,7 +48,10 @@ namespace tdt {
 
 constexpr int kSupBlock = 512;                 // 16 warps
 constexpr int kSupWarps = kSupBlock / kWarp;
-constexpr int kSupMinBlocks = 3;               // resident blocks per SM (registers <= 42)
+#ifndef TDT_SUP_MINB
+#define TDT_SUP_MINB 3
+#endif
+constexpr int kSupMinBlocks = TDT_SUP_MINB;    // resident blocks per SM (3: registers <= 42)
 constexpr int kSupSmemBytes = 64 * 1024;       // dynamic shared memory per block
 constexpr int kVertexBatch = 2;                // light vertices per grab below the top quarter of ids
 constexpr int kHeavyChunk = 16;                // vertices scanned per heavy grab

@@ -45,7 +45,10 @@ namespace tdt {
 
 constexpr int kTrBlock = 512;
 constexpr int kTrWarps = kTrBlock / kWarp;
-constexpr int kTrMinBlocks = 3;
+#ifndef TDT_TR_MINB
+#define TDT_TR_MINB 3
+#endif
+constexpr int kTrMinBlocks = TDT_TR_MINB;
 constexpr int kTrSmemCur = 3072;   // out-edge cursors a group keeps in shared memory (24 KB)
 #ifndef TDT_TR_KEYED
 #define TDT_TR_KEYED 1
