@@ -713,7 +713,8 @@ __device__ __forceinline__ void window_items(const long long* __restrict__ qb, c
 // The other two edges (f, g) of slot tl of item it; false when the slot is
 // not a triangle (search mode only).
 template <bool Listed>
-__device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, long long tl, int32_t& f, int32_t& g) {
+__device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, long long tl, int r, int32_t& f,
+                                           int32_t& g) {
     if (Listed) {
         const long long lo = (long long)(unsigned)it.y | ((long long)it.z << 32);
         const int2 fg = __ldg(A.lists + lo + tl);
@@ -732,7 +733,15 @@ __device__ __forceinline__ bool slot_edges(const PeelArgs& A, const int4& it, lo
         f = __ldg(A.in_eid + kk);
     }
     if (w == y) return false;
-    if (kDeadFilter && ((A.dead[f >> 5] >> (f & 31)) & 1u)) return false;  // (x,w) peeled before this round
+    if (kPeelCodes) {
+        // no search when (x,w) was peeled before this round, or peels in it
+        // too with the smaller index: then the other edge of the triangle is
+        // decremented from (x,w)'s own slot, not from this one
+        const int32_t cf = code_round(__ldcg(A.code + (f >> 3)), f, r);
+        if (cf == -2 || (cf == r && it.x > f)) return false;
+    } else if (kDeadFilter && ((A.dead[f >> 5] >> (f & 31)) & 1u)) {
+        return false;  // (x,w) peeled before this round
+    }
     const int64_t gg = (w < y) ? find_sorted<int64_t>(A.cols, __ldg(A.rp + w), __ldg(A.rp + w + 1), y)
                                : find_sorted<int64_t>(A.cols, __ldg(A.rp + y), __ldg(A.rp + y + 1), w);
     g = (int32_t)gg;
@@ -876,7 +885,7 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
             f[h] = 0;
             g[h] = 0;
             tr[h] = false;
-            if (v[h]) tr[h] = slot_edges<Listed>(A, it[h], cb + h * kWarp + lane - bl[h], f[h], g[h]);
+            if (v[h]) tr[h] = slot_edges<Listed>(A, it[h], cb + h * kWarp + lane - bl[h], r, f[h], g[h]);
         }
         int32_t rf[kWin], rg[kWin];
 #pragma unroll
