@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--lists", choices=["auto", "on", "off"], default="auto",
+                    help="triangle lists of the main decomposition: auto (whenever they fit), on, or off (the search "
+                         "peel, as on graphs whose lists do not fit)")
     ap.add_argument("--cpu-scale", type=int, default=0, help="R-MAT scale of the CPU sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -773,6 +776,7 @@ def main_ours(args):
     L = _lib.load()  # raises if the CUDA library is missing
 
     scale, ef = args.scale, args.edge_factor
+    lists_arg = {"auto": "auto", "on": True, "off": False}[args.lists]
     m = ef << scale
     src, dst = G.rmat_edges_device(scale, m, seed=1, device=dev)
     g, vertices = preprocess_edges(src, dst)
@@ -797,13 +801,13 @@ def main_ours(args):
     wsp = T.Workspace(dev)
 
     def step():
-        return T.truss_decompose(g, workspace=wsp, sync=False)
+        return T.truss_decompose(g, workspace=wsp, sync=False, lists=lists_arg)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     # correctness anchor of this run: stats of one decomposition
-    res = T.truss_decompose(g, workspace=wsp)
+    res = T.truss_decompose(g, workspace=wsp, lists=lists_arg)
 
     clocks = ClockSampler(local) if rank == 0 else None
     if clocks:
@@ -848,7 +852,8 @@ def main_ours(args):
     def e2e_step():
         d_cols.copy_(cols_h, non_blocking=True)
         d_rp.copy_(rp_h, non_blocking=True)
-        tr, _, _, st = T.truss_decompose(CSRCOO(columns=d_cols, row_ptr=d_rp), workspace=wsp, sync=False)
+        tr, _, _, st = T.truss_decompose(CSRCOO(columns=d_cols, row_ptr=d_rp), workspace=wsp, sync=False,
+                                         lists=lists_arg)
         truss_h.copy_(tr, non_blocking=True)
         e2e_stats.append(st)
 
@@ -884,6 +889,9 @@ def main_ours(args):
     # then one re-enumeration of each edge's triangles (listing + peel)
     mt = TRAFFIC_BY_WORKLOAD.get((scale, ef)) or {k: v * res.triangles for k, v in TRAFFIC_PER_TRIANGLE.items()}
     traffic_src = TRAFFIC_SOURCE_BY_WORKLOAD if (scale, ef) in TRAFFIC_BY_WORKLOAD else TRAFFIC_SOURCE
+    if res.listing != 2:
+        # the captures behind these figures are of the one-walk listed path
+        mt, traffic_src = None, "not captured for this path"
     B_dec = 2 * B_sup
     ach = B_dec / (ms_step / 1e3) / 1e9
     phases_ms = {"support": t_sup, "listing": t_list, "peel": t_peel, "outputs": t_post}
