@@ -91,9 +91,9 @@ struct PeelArgs {
     int4* qi[3];
     long long* qb[3];
     int32_t* alive[2];    // compacted alive-edge lists (level transitions)
-    // bit e set: edge e was peeled in a sub-round before the current one (the
-    // search peel's filter in L2 before a candidate's binary search; a bit not
-    // set yet only costs the search it would have saved)
+    // bit e set: edge e was peeled in a sub-round before the current one (a
+    // filter in L2 before the state checks, used only in builds without the
+    // round codes; a bit not set yet only costs the check it would have saved)
     unsigned* dead;
     // round code of edge e in the 4 bits at (e & 7) * 4 of word e >> 3 (the
     // listed peel's partner-state check; see code_round)
@@ -810,16 +810,18 @@ __device__ __forceinline__ void process_round(const PeelArgs& A, int r, int32_t 
     const long long T = (long long)(packed & kCandMask);
     const long long* __restrict__ qb = A.qb[buf];
     const int4* __restrict__ qi = A.qi[buf];
-    // the edges of round r-1 are dead from this round on: set their bits (a
-    // bit read before it is set only sends that triangle to the state check)
-    if (kDeadFilter && r > 0) {
+    // the edges of round r-1 are dead from this round on: their round codes
+    // turn dead (needed by round r+2, where (r-1) & 3 would read "marked for
+    // the next round"), or, without the codes, their dead bits are set (a bit
+    // read before it is set only sends that triangle to the state check)
+    if ((kPeelCodes || kDeadFilter) && r > 0) {
         long long nprev = (long long)(ld_cg_u64(&A.ctl->q[(r - 1) & 3]) >> kCandBits);
         if (nprev > A.E) nprev = A.E;
         const int4* __restrict__ qp = A.qi[(r - 1) % 3];
         for (long long i = gwarp * kWarp + lane; i < nprev; i += nwarps * kWarp) {
             const int32_t e = __ldcg(&qp[i].x);
-            atomicOr(A.dead + (e >> 5), 1u << (e & 31));
-            atomicOr(A.code + (e >> 3), kCodeDead << ((unsigned)(e & 7) * 4u));
+            if (kPeelCodes) atomicOr(A.code + (e >> 3), kCodeDead << ((unsigned)(e & 7) * 4u));
+            else atomicOr(A.dead + (e >> 5), 1u << (e & 31));
         }
     }
     // listed mode: each warp owns a contiguous range of candidate slots (a
